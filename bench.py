@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark: ensemble trajectories/sec at a fixed FP64-oracle error on one GB300.
+
+Workload (the adaptive Lorenz ensemble): 1,048,576 trajectories of the Lorenz system,
+u0 = [1,0,0] + N(0, 0.1^2), p = U(0,1)^3 .* [10, 28, 8/3], tspan (0, 10), saveat 0:0.5:10,
+GPUTsit5 adaptive, reltol 1e-6, abstol 1e-8, initial dt 0.1, FP32 state with FP64 time;
+seeded synthetic inputs.  A step is one full ensemble solve (one CUDA-graph launch of the
+persistent kernel).  Lines printed (rank 0, one JSON line):
+  value      trajectories/s with inputs resident in HBM (device-timed, L2 flushed between steps)
+  e2e        the same through the C ABI with host buffers (degpu_batch_solve_host: H2D of
+             u0/p/tspan/saveat and D2H of ts/us/retcode inside the timed region)
+  roofline   FP32 FLOP/s of the stepping kernel (algorithmic flops from the per-trajectory
+             accept/reject counters) against a live FP32-FMA peak measurement
+  cpu_baseline  the oracle's C++ restatement of the reference's kernel path on the host cores
+  oracle_error  final-state relative error vs an FP64 Vern9 solution at reltol 1e-12
+`--impl reference` times the reference's CPU path (its C++ restatement -- the Julia
+reference cannot run here) on all host cores, on bounded samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "diffeqgpu.jl_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+WORKLOAD = dict(name="lorenz_adaptive_tsit5_saveat21", B=1 << 20, tspan=(0.0, 10.0), saveat_step=0.5,
+                reltol=1e-6, abstol=1e-8, dt=0.1, alg="tsit5", model="lorenz", seed=20261204)
+METRIC = "trajectories/sec at fixed FP64-oracle error: learned-dt vs plain, 1 GB300"
+
+
+def make_inputs(B, seed, offset=0):
+    rng = np.random.default_rng(seed)
+    if offset:
+        rng.random((offset, 3))
+        rng.normal(0, 0.1, (offset, 3))
+    p = (rng.random((B, 3)) * np.array([10, 28, 8 / 3])).astype(np.float32)
+    u0 = (np.array([1, 0, 0]) + rng.normal(0, 0.1, (B, 3))).astype(np.float32)
+    return u0, p
+
+
+def saveat_grid():
+    return np.arange(0.0, WORKLOAD["tspan"][1] + 1e-9, WORKLOAD["saveat_step"])
+
+
+def nproc():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------------ CPU side (oracle = C++ restatement)
+def cpu_rate(u0, p, sample, threads):
+    import oracle
+    sa = saveat_grid()
+    t = time.perf_counter()
+    oracle.solve(WORKLOAD["model"], WORKLOAD["alg"], u0[:sample], p[:sample], list(WORKLOAD["tspan"]), adaptive=True,
+                 dt=WORKLOAD["dt"], L=len(sa), saveat=sa, abstol=WORKLOAD["abstol"], reltol=WORKLOAD["reltol"],
+                 time_f64=True, nthreads=threads)
+    return sample / (time.perf_counter() - t)
+
+
+def calibrate_sample(u0, p, threads, target_s):
+    r = cpu_rate(u0, p, 2048, threads)
+    return int(max(2048, min(len(u0), r * target_s))), r
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU path (C++ restatement) on all host cores."""
+    import oracle
+    oracle.build()
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = nproc()
+    u0, p = make_inputs(WORKLOAD["B"], WORKLOAD["seed"])
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    sample, _ = calibrate_sample(u0, p, threads, min(20.0, budget))
+    for _ in range(args.warmup):
+        cpu_rate(u0, p, sample, threads)
+    rates = [cpu_rate(u0, p, sample, threads) for _ in range(args.steps)]
+    v = float(np.mean(rates))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "trajectories/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sample / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 state / f64 time", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD["name"], "trajectories": WORKLOAD["B"], "alg": "Tsit5 (adaptive)",
+                       "reltol": WORKLOAD["reltol"], "abstol": WORKLOAD["abstol"], "saveat": "0:0.5:10",
+                       "parallelism": "OpenMP over trajectories"},
+            "cpu_baseline": {"value": v, "unit": "trajectories/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample} of the {WORKLOAD['B']} trajectories per step"},
+            "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(", ") for r in self.path.read_text().strip().splitlines() if r.strip()]
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in rows for j in range(4) if len(r) > 5 + j and r[5 + j].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ oracle error
+def oracle_error(u0, p, us_final, idx):
+    """Final-state relative error at t=10 against FP64 Vern9 (reltol 1e-12), over the
+    members whose FP64 solution is stable under a 1e-10 perturbation of u0."""
+    import oracle
+    u = u0[idx].astype(np.float64)
+    pp = p[idx].astype(np.float64)
+    tf = np.array([WORKLOAD["tspan"][1]])
+    ref, _ = oracle.vern9("lorenz", u, pp, 0.0, tf, rtol=1e-12, atol=1e-14)
+    pert, _ = oracle.vern9("lorenz", u * (1 + 1e-10), pp, 0.0, tf, rtol=1e-12, atol=1e-14)
+    ref, pert = ref[:, 0], pert[:, 0]
+    nref = np.maximum(np.linalg.norm(ref, axis=1), 1e-3)
+    stable = np.linalg.norm(ref - pert, axis=1) / nref < 1e-6
+    err = np.linalg.norm(us_final[idx].astype(np.float64) - ref, axis=1) / nref
+    e = err[stable]
+    return {"median": float(np.median(e)), "p90": float(np.quantile(e, 0.9)), "max": float(e.max()),
+            "n_sample": int(len(idx)), "n_stable": int(stable.sum()),
+            "excluded_frac": float(1 - stable.mean()), "bar": 1e-4,
+            "meets_bar_p90": bool(np.quantile(e, 0.9) <= 1e-4)}
+
+
+# ------------------------------------------------------------------ GPU arm
+def gpu_arm(args):
+    import torch
+
+    import degpu
+    from degpu import _lib, flops
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    B = args.trajectories or WORKLOAD["B"]
+    u0, p = make_inputs(B, WORKLOAD["seed"] + rank)
+    sa = saveat_grid()
+    L = len(sa)
+    f = degpu.ODEFunction.builtin("lorenz")
+    tsp = np.tile(np.array(WORKLOAD["tspan"], np.float64), (B, 1))
+    probs = degpu.DeviceProblems(f, u0, p, tsp, np.float64, dev)
+    sa_dev = torch.as_tensor(sa, device=dev)
+    ts = torch.empty((B, L), dtype=torch.float64, device=dev)
+    us = torch.empty((B, L, 3), dtype=torch.float32, device=dev)
+    rc = torch.empty(B, dtype=torch.int8, device=dev)
+    na = torch.empty(B, dtype=torch.int32, device=dev)
+    nr = torch.empty(B, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    opt = degpu.api._options(degpu.GPUTsit5(), np.float64, dt=WORKLOAD["dt"], abstol=WORKLOAD["abstol"],
+                             reltol=WORKLOAD["reltol"], saveat_dev=sa_dev.data_ptr(), nsaveat=L, driver="persistent",
+                             traj_offset=rank * B)
+    out = _lib.Outputs(ts.data_ptr(), us.data_ptr(), L, rc.data_ptr(), na.data_ptr(), nr.data_ptr())
+    pr = probs.cstruct()
+    plan = ctypes.c_void_p()
+    _lib.check(_lib.lib().degpu_plan_create(f.handle(), ctypes.byref(pr), ctypes.byref(opt), 1, ctypes.byref(out),
+                                            sptr, ctypes.byref(plan)))
+    info = [ctypes.c_int() for _ in range(5)]
+    _lib.check(_lib.lib().degpu_plan_info(plan, *[ctypes.byref(x) for x in info]))
+    block, chunk, grid, driver, regs = [x.value for x in info]
+    peak = ctypes.c_double()
+    _lib.check(_lib.lib().degpu_fp32_peak(ctypes.byref(peak), sptr))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    for _ in range(args.warmup):
+        _lib.check(_lib.lib().degpu_plan_launch(plan, sptr))
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    times = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(dev)
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (256 MiB > 129 MB L2), outside the events
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(_lib.lib().degpu_plan_launch(plan, sptr))
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - wall0
+    tot_ms = float(np.sum(times))
+    if dist:
+        t = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+        dist.barrier()
+    value = B * world * args.steps / (tot_ms * 1e-3)
+
+    # per-launch algorithmic flops from the counters of the last solve
+    na_h, nr_h, rc_h = na.cpu().numpy(), nr.cpu().numpy(), rc.cpu().numpy()
+    us_h = us.cpu().numpy()
+    fl = flops.solve_flops("tsit5", 3, "lorenz", na_h, nr_h, nsaves=B * L)
+    kern_ms = tot_ms / args.steps
+    achieved = fl / (kern_ms * 1e-3) / 1e12
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        hu0, hp, htsp, hsa = pin(u0), pin(p), pin(tsp), pin(sa)
+        hts = torch.empty((B, L), dtype=torch.float64).pin_memory()
+        hus = torch.empty((B, L, 3), dtype=torch.float32).pin_memory()
+        hrc = torch.empty(B, dtype=torch.int8).pin_memory()
+        hopt = degpu.api._options(degpu.GPUTsit5(), np.float64, dt=WORKLOAD["dt"], abstol=WORKLOAD["abstol"],
+                                  reltol=WORKLOAD["reltol"], saveat_dev=hsa.data_ptr(), nsaveat=L, driver="persistent",
+                                  block=block, chunk=chunk)
+
+        def e2e_step():
+            _lib.check(_lib.lib().degpu_batch_solve_host(f.handle(), hu0.data_ptr(), hp.data_ptr(), htsp.data_ptr(), B,
+                                                         ctypes.byref(hopt), 1, hts.data_ptr(), hus.data_ptr(), L,
+                                                         hrc.data_ptr(), None, None, sptr))
+        for _ in range(min(args.warmup, 2)):
+            e2e_step()
+        k = max(1, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(k):
+            e2e_step()
+        e2e_s = (time.perf_counter() - t0) / k
+        h2d = hu0.numel() * 4 + hp.numel() * 4 + htsp.numel() * 8 + hsa.numel() * 8
+        d2h = hts.numel() * 8 + hus.numel() * 4 + hrc.numel()
+        same = np.array_equal(hus.numpy().view(np.uint32), us_h.view(np.uint32))
+        e2e = {"value": B / e2e_s, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3, "api": "degpu_batch_solve_host",
+               "matches_device_run": bool(same)}
+
+    if rank != 0:
+        _lib.lib().degpu_plan_destroy(plan)
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # oracle error (FP64 Vern9) on a fixed sample
+    idx = np.arange(0, B, max(1, B // 2048))[:2048]
+    err = oracle_error(u0, p, us_h[:, -1, :], idx)
+
+    # CPU baseline: the oracle's restatement of the reference path, all host cores, bounded sample
+    threads = nproc()
+    cpu = None
+    if not args.no_cpu:
+        sample, _ = calibrate_sample(u0, p, threads, 10.0)
+        rate = cpu_rate(u0, p, sample, threads)
+        cpu = {"value": rate, "unit": "trajectories/s", "cores": threads, "kind": "port",
+               "sample": f"first {sample} of the {B} trajectories, same workload, OpenMP over trajectories"}
+
+    traffic = None
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        try:
+            tj = json.loads(prof.read_text())
+            traffic = tj.get("persistent_tsit5_lorenz_bytes_per_traj")
+            if traffic is not None:
+                traffic = traffic * B
+        except Exception:
+            traffic = None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 state / f64 time", "data": "synthetic (seeded)",
+        "method": "plain PI controller, persistent warp-refill driver, CUDA graph",
+        "config": {"workload": WORKLOAD["name"], "trajectories": B, "alg": "GPUTsit5 (adaptive)",
+                   "reltol": WORKLOAD["reltol"], "abstol": WORKLOAD["abstol"], "saveat": "0:0.5:10",
+                   "tspan": list(WORKLOAD["tspan"]), "l2": "flushed between timed steps (256 MiB memset)",
+                   "parallelism": "one process per GPU, trajectories sharded" if world > 1 else "single GPU",
+                   "block": block, "chunk": chunk, "grid": grid, "regs_per_thread": regs},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                     "frac": achieved / peak.value, "traffic": traffic,
+                     "peak_source": "measured live: FP32 FMA probe (degpu_fp32_peak)",
+                     "flops_per_launch": fl, "attempts_per_traj": float((na_h + nr_h).mean()),
+                     "reject_frac": float(nr_h.sum() / max(1, (na_h + nr_h).sum()))},
+        "oracle_error": err,
+        "retcodes_ok": bool((rc_h == 1).all()),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "gpu_launches": args.steps,
+        "wall_s_timed_region": wall,
+        "clocks": clk.summary(),
+    }
+    _lib.lib().degpu_plan_destroy(plan)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="degpu", choices=["degpu", "reference"])
+    ap.add_argument("--trajectories", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

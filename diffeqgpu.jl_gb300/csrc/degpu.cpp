@@ -1,0 +1,698 @@
+// libdegpu: host side of the GB300 EnsembleGPUKernel engine (C ABI in include/degpu.h).
+//
+// Replaces the reference's lower-level kernel API (src/ensemblegpukernel/lowerlevel_solve.jl)
+// and its launch of ode_solve_kernel / ode_asolve_kernel / em_kernel (kernels.jl,
+// perform_step/gpu_em_perform_step.jl).  Each (right-hand side, algorithm, driver, time
+// type, mode) combination is one NVRTC translation unit: the user's CUDA C right-hand
+// side followed by the stepper/driver templates, compiled for sm_103a, cached in memory
+// and on disk, loaded once per device.  Launches are stream-ordered; plans capture the
+// whole solve in a CUDA graph.
+#include "degpu.h"
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <sys/stat.h>
+#include <unistd.h>
+#include <vector>
+
+#include "device/degpu_params.h"
+
+// embedded device sources (generated by build.py from csrc/device and csrc/models)
+struct degpu_embedded_file { const char* name; const char* text; };
+struct degpu_embedded_model { const char* name; int n, p, flags; const char* text; };
+extern "C" const degpu_embedded_file degpu_embedded_headers[];
+extern "C" const int degpu_embedded_nheaders;
+extern "C" const degpu_embedded_model degpu_embedded_models[];
+extern "C" const int degpu_embedded_nmodels;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+#define CU_TRY(expr)                                                                   \
+  do {                                                                                 \
+    CUresult _r = (expr);                                                              \
+    if (_r != CUDA_SUCCESS) {                                                          \
+      const char* _s = nullptr;                                                        \
+      if (g_drv.GetErrorString) g_drv.GetErrorString(_r, &_s);                         \
+      return fail(DEGPU_E_CUDA, std::string(#expr) + ": " + (_s ? _s : "CUDA error")); \
+    }                                                                                  \
+  } while (0)
+#define CUDA_TRY(expr)                                                                       \
+  do {                                                                                       \
+    cudaError_t _e = (expr);                                                                 \
+    if (_e != cudaSuccess) return fail(DEGPU_E_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+// Driver-API entry points, resolved at run time through the CUDA runtime
+// (cudaGetDriverEntryPointByVersion) so that the library loads on machines without a
+// driver (build and CPU-only test hosts) and needs no link against libcuda.
+struct Driver {
+  CUresult (*ModuleLoadData)(CUmodule*, const void*) = nullptr;
+  CUresult (*ModuleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
+  CUresult (*LaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                           CUstream, void**, void**) = nullptr;
+  CUresult (*FuncGetAttribute)(int*, CUfunction_attribute, CUfunction) = nullptr;
+  CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
+  CUresult (*GetErrorString)(CUresult, const char**) = nullptr;
+  bool ok = false;
+};
+Driver g_drv;
+
+template <class F>
+bool resolve(const char* name, F*& fn) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult st;
+  if (cudaGetDriverEntryPointByVersion(name, &p, 13000, cudaEnableDefault, &st) != cudaSuccess || !p) return false;
+  fn = reinterpret_cast<F*>(p);
+  return true;
+}
+
+int load_driver() {
+  static std::once_flag once;
+  static std::string err;
+  std::call_once(once, [] {
+    cudaError_t e = cudaFree(0);
+    if (e != cudaSuccess) { err = std::string("CUDA initialisation failed: ") + cudaGetErrorString(e); return; }
+    bool ok = resolve("cuModuleLoadData", g_drv.ModuleLoadData) && resolve("cuModuleGetFunction", g_drv.ModuleGetFunction) &&
+              resolve("cuLaunchKernel", g_drv.LaunchKernel) && resolve("cuFuncGetAttribute", g_drv.FuncGetAttribute) &&
+              resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", g_drv.OccupancyMaxActiveBlocksPerMultiprocessor) &&
+              resolve("cuGetErrorString", g_drv.GetErrorString);
+    if (!ok) err = "could not resolve CUDA driver entry points";
+    g_drv.ok = ok;
+  });
+  if (!g_drv.ok) return fail(DEGPU_E_CUDA, err);
+  return 0;
+}
+
+uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ULL) {
+  for (unsigned char c : s) { h ^= c; h *= 1099511628211ULL; }
+  return h;
+}
+
+}  // namespace
+
+struct degpu_rhs_s {
+  std::string src;
+  int N, P, flags;
+};
+
+namespace {
+
+struct KernelSpec {
+  int alg, driver, tt, parity, jac, tgrad, refine;
+  std::string key() const {
+    char b[128];
+    snprintf(b, sizeof b, "a%d_d%d_t%d_m%d_j%d_g%d_r%d", alg, driver, tt, parity, jac, tgrad, refine);
+    return b;
+  }
+};
+
+struct Kernel {
+  CUfunction fn = nullptr;
+  int regs = 0, local_bytes = 0, max_threads = 0;
+};
+
+std::mutex g_mu;
+std::map<std::string, std::vector<char>> g_cubins;  // source-key -> cubin
+std::map<std::string, CUmodule> g_modules;          // source-key + device -> module
+std::map<std::string, Kernel> g_kernels;
+std::map<std::string, std::pair<int, int>> g_tuned;  // autotune cache
+
+std::string cache_dir() {
+  const char* d = getenv("DEGPU_CACHE_DIR");
+  std::string dir;
+  if (d && *d) dir = d;
+  else {
+    const char* h = getenv("HOME");
+    dir = std::string(h && *h ? h : "/tmp") + "/.cache/degpu";
+  }
+  return dir;
+}
+
+void mkdirs(const std::string& path) {
+  std::string cur;
+  for (size_t i = 0; i < path.size(); i++) {
+    cur += path[i];
+    if (path[i] == '/' && cur.size() > 1) mkdir(cur.c_str(), 0755);
+  }
+  mkdir(path.c_str(), 0755);
+}
+
+std::string build_source(const degpu_rhs_s* f, const KernelSpec& k) {
+  char defs[512];
+  snprintf(defs, sizeof defs,
+           "#define DEGPU_N %d\n#define DEGPU_P %d\n#define DEGPU_TT %s\n#define DEGPU_ALG %d\n"
+           "#define DEGPU_DRIVER %d\n#define DEGPU_PARITY %d\n#define DEGPU_JAC %d\n#define DEGPU_TGRAD %d\n"
+           "#define DEGPU_LINSOLVE_REFINE %d\n",
+           f->N, f->P, k.tt ? "double" : "float", k.alg, k.driver, k.parity, k.jac, k.tgrad, k.refine);
+  std::string s = defs;
+  s += "#include \"degpu_prelude.cuh\"\n#line 1 \"user_rhs.cu\"\n";
+  s += f->src;
+  s += "\n#include \"degpu_kernels.cuh\"\n";
+  return s;
+}
+
+int compile_cubin(const std::string& src, bool parity, std::vector<char>& cubin) {
+  int major = 0, minor = 0;
+  nvrtcVersion(&major, &minor);
+  std::string opts_key = std::string(parity ? "fmad0" : "fmad1") + "|sm_103a|" + std::to_string(major) + "." + std::to_string(minor);
+  uint64_t h = fnv1a(opts_key, fnv1a(src));
+  char hex[32];
+  snprintf(hex, sizeof hex, "%016llx", (unsigned long long)h);
+  std::string path = cache_dir() + "/" + hex + ".cubin";
+  if (!getenv("DEGPU_NO_DISK_CACHE")) {
+    FILE* fp = fopen(path.c_str(), "rb");
+    if (fp) {
+      fseek(fp, 0, SEEK_END);
+      long n = ftell(fp);
+      fseek(fp, 0, SEEK_SET);
+      if (n > 0) {
+        cubin.resize(n);
+        size_t got = fread(cubin.data(), 1, n, fp);
+        fclose(fp);
+        if ((long)got == n) return 0;
+      } else {
+        fclose(fp);
+      }
+    }
+  }
+  std::vector<const char*> hdr_txt, hdr_names;
+  for (int i = 0; i < degpu_embedded_nheaders; i++) {
+    hdr_names.push_back(degpu_embedded_headers[i].name);
+    hdr_txt.push_back(degpu_embedded_headers[i].text);
+  }
+  nvrtcProgram prog;
+  nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "degpu_tu.cu", (int)hdr_txt.size(), hdr_txt.data(), hdr_names.data());
+  if (r != NVRTC_SUCCESS) return fail(DEGPU_E_COMPILE, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
+  std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo",
+                                   parity ? "--fmad=false" : "--fmad=true", "--prec-div=true", "--prec-sqrt=true"};
+  r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
+  if (r != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string log(n, '\0');
+    nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcDestroyProgram(&prog);
+    return fail(DEGPU_E_COMPILE, "NVRTC compile failed:\n" + log);
+  }
+  size_t n = 0;
+  nvrtcGetCUBINSize(prog, &n);
+  cubin.resize(n);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  if (!getenv("DEGPU_NO_DISK_CACHE")) {
+    mkdirs(cache_dir());
+    std::string tmp = path + ".tmp" + std::to_string(getpid());
+    FILE* fp = fopen(tmp.c_str(), "wb");
+    if (fp) {
+      fwrite(cubin.data(), 1, n, fp);
+      fclose(fp);
+      rename(tmp.c_str(), path.c_str());
+    }
+  }
+  return 0;
+}
+
+const char* kernel_name(int driver) {
+  switch (driver) {
+    case 2: return "degpu_persistent_kernel";
+    case 3: return "degpu_em_kernel";
+    default: return "degpu_solve_kernel";
+  }
+}
+
+int ensure_context() {
+  int rc = load_driver();
+  if (rc) return rc;
+  CUDA_TRY(cudaFree(0));  // makes the runtime's primary context of the current device current
+  return 0;
+}
+
+int get_kernel(const degpu_rhs_s* f, const KernelSpec& k, Kernel* out) {
+  int rc = ensure_context();
+  if (rc) return rc;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  std::string src = build_source(f, k);
+  std::string skey = std::to_string(fnv1a(src)) + "|" + k.key();
+  std::string mkey = skey + "|dev" + std::to_string(dev);
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_kernels.find(mkey);
+  if (it != g_kernels.end()) { *out = it->second; return 0; }
+  auto cit = g_cubins.find(skey);
+  if (cit == g_cubins.end()) {
+    std::vector<char> cubin;
+    rc = compile_cubin(src, k.parity != 0, cubin);
+    if (rc) return rc;
+    cit = g_cubins.emplace(skey, std::move(cubin)).first;
+  }
+  CUmodule mod;
+  CU_TRY(g_drv.ModuleLoadData(&mod, cit->second.data()));
+  g_modules[mkey] = mod;
+  Kernel kern;
+  CU_TRY(g_drv.ModuleGetFunction(&kern.fn, mod, kernel_name(k.driver)));
+  g_drv.FuncGetAttribute(&kern.regs, CU_FUNC_ATTRIBUTE_NUM_REGS, kern.fn);
+  g_drv.FuncGetAttribute(&kern.local_bytes, CU_FUNC_ATTRIBUTE_LOCAL_SIZE_BYTES, kern.fn);
+  g_drv.FuncGetAttribute(&kern.max_threads, CU_FUNC_ATTRIBUTE_MAX_THREADS_PER_BLOCK, kern.fn);
+  g_kernels[mkey] = kern;
+  *out = kern;
+  return 0;
+}
+
+// ------------------------------------------------------------------ request validation
+struct Request {
+  const degpu_rhs_s* f;
+  KernelSpec spec;
+  degpu_kparams kp;
+  int block, chunk;
+};
+
+int resolve_driver(const degpu_options* o, int adaptive) {
+  if (o->alg == DEGPU_ALG_EM) return 3;
+  if (!adaptive) return 0;
+  if (o->driver == DEGPU_DRIVER_NAIVE) return 1;
+  return 2;
+}
+
+int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_options* o, int adaptive,
+                 const degpu_outputs* out, Request* rq) {
+  if (!f || !pr || !o || !out) return fail(DEGPU_E_INVALID, "null argument");
+  if (pr->B < 0) return fail(DEGPU_E_INVALID, "negative trajectory count");
+  if (pr->B > 0x7fffffffLL) return fail(DEGPU_E_INVALID, "more than 2^31-1 trajectories in one call; split into batches");
+  if (o->alg < 0 || o->alg > 4) return fail(DEGPU_E_INVALID, "unknown algorithm");
+  if (o->alg == DEGPU_ALG_EM && adaptive)
+    return fail(DEGPU_E_UNSUPPORTED, "Adaptive time-stepping is not supported yet with GPUEM.");
+  if (o->alg == DEGPU_ALG_EM && !(f->flags & DEGPU_RHS_HAS_NOISE))
+    return fail(DEGPU_E_INVALID, "GPUEM needs a right-hand side with a noise function (DEGPU_RHS_HAS_NOISE)");
+  if (o->time_type != DEGPU_TIME_F32 && o->time_type != DEGPU_TIME_F64) return fail(DEGPU_E_INVALID, "time_type");
+  if (o->mode != DEGPU_MODE_FAST && o->mode != DEGPU_MODE_PARITY) return fail(DEGPU_E_INVALID, "mode");
+  if (!(o->dt > 0.0) && !o->dt0) return fail(DEGPU_E_INVALID, "dt must be positive");
+  if (out->L < 1) return fail(DEGPU_E_INVALID, "L must be >= 1");
+  if (o->nsaveat < 0) return fail(DEGPU_E_INVALID, "nsaveat < 0");
+  if (o->nsaveat > 0 && !o->saveat) return fail(DEGPU_E_INVALID, "saveat pointer missing");
+  if (o->nsaveat > 0 && out->L != o->nsaveat)
+    return fail(DEGPU_E_INVALID, "L must equal the number of saveat points (lowerlevel_solve.jl:106, 321)");
+  if (o->nsaveat == 0 && !o->save_everystep && out->L != 2)
+    return fail(DEGPU_E_INVALID, "without saveat and with save_everystep=false the output has L=2 rows (lowerlevel_solve.jl:79, 315)");
+  if (pr->B > 0 && (!pr->u0 || !pr->tspan || !out->ts || !out->us)) return fail(DEGPU_E_INVALID, "null device buffer");
+  if (pr->B > 0 && f->P > 0 && !pr->p) return fail(DEGPU_E_INVALID, "null parameter buffer");
+  if (o->block < 0 || o->block > 1024 || (o->block % 32) != 0) return fail(DEGPU_E_INVALID, "block must be a multiple of 32 in [32, 1024]");
+  if (o->chunk < 0 || o->chunk > 4096) return fail(DEGPU_E_INVALID, "chunk must be in [0, 4096]");
+  rq->f = f;
+  KernelSpec& k = rq->spec;
+  k.alg = o->alg;
+  k.driver = resolve_driver(o, adaptive);
+  k.tt = o->time_type;
+  k.parity = o->mode == DEGPU_MODE_PARITY;
+  int jac_user = (f->flags & DEGPU_RHS_HAS_JAC) ? 1 : 0, tg_user = (f->flags & DEGPU_RHS_HAS_TGRAD) ? 1 : 0;
+  if (o->jac == DEGPU_JAC_AUTO) { k.jac = jac_user ? 1 : 0; k.tgrad = tg_user ? 1 : 0; }
+  else if (o->jac == DEGPU_JAC_AD) { k.jac = 0; k.tgrad = 0; }
+  else if (o->jac == DEGPU_JAC_FINITEDIFF) { k.jac = 2; k.tgrad = 2; }
+  else return fail(DEGPU_E_INVALID, "jac");
+  if (o->alg != DEGPU_ALG_ROSENBROCK23 && o->alg != DEGPU_ALG_RODAS5P) { k.jac = 0; k.tgrad = 0; }
+  k.refine = (o->alg == DEGPU_ALG_ROSENBROCK23 || o->alg == DEGPU_ALG_RODAS5P) && !k.parity ? 1 : 0;
+  degpu_kparams& P = rq->kp;
+  memset(&P, 0, sizeof P);
+  P.u0 = pr->u0;
+  P.p = pr->p;
+  P.tspan = pr->tspan;
+  P.saveat = o->nsaveat ? o->saveat : nullptr;
+  P.ts = out->ts;
+  P.us = out->us;
+  P.retcode = out->retcode;
+  P.naccept = out->naccept;
+  P.nreject = out->nreject;
+  P.dt0 = o->dt0;
+  P.tolscale = o->tolscale;
+  P.B = pr->B;
+  P.maxiters = o->maxiters > 0 ? o->maxiters : 10000000LL;
+  P.traj_offset = o->traj_offset;
+  P.seed = o->seed;
+  P.dt = o->dt;
+  P.abstol = (float)o->abstol;
+  P.reltol = (float)o->reltol;
+  P.L = out->L;
+  P.nsaveat = o->nsaveat;
+  P.saveat_per_traj = o->saveat_per_traj;
+  P.save_everystep = o->save_everystep;
+  rq->block = o->block;
+  rq->chunk = o->chunk;
+  return 0;
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+int grid_for(const Request& rq, const Kernel& K, int block) {
+  long long B = rq.kp.B;
+  if (rq.spec.driver != 2) return (int)((B + block - 1) / block);
+  // persistent: fill the machine once (a multiple of the SM count), never more than needed
+  int per_sm = 0;
+  g_drv.OccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, K.fn, block, 0);
+  if (per_sm < 1) per_sm = 1;
+  long long g = (long long)per_sm * sm_count();
+  long long need = (B + block - 1) / block;
+  return (int)std::max(1LL, std::min(g, need));
+}
+
+int default_block(const Request& rq) { return rq.spec.driver == 2 ? 128 : 128; }
+int default_chunk() { return 32; }
+
+int launch(const Request& rq, const Kernel& K, int block, int chunk, unsigned long long* work, CUstream s) {
+  degpu_kparams P = rq.kp;
+  P.chunk = chunk;
+  P.work = work;
+  int grid = grid_for(rq, K, block);
+  if (rq.spec.driver == 2) {
+    if (!work) return fail(DEGPU_E_INVALID, "persistent driver without a work counter");
+    CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(unsigned long long), (cudaStream_t)s));
+  }
+  void* args[] = {(void*)&P};
+  CU_TRY(g_drv.LaunchKernel(K.fn, grid, 1, 1, block, 1, 1, 0, s, args, nullptr));
+  return 0;
+}
+
+// Stream-ordered solve with a per-call work counter from the stream-ordered allocator.
+int run(const degpu_rhs* f, const degpu_problems* pr, const degpu_options* o, int adaptive, degpu_outputs* out, void* stream) {
+  Request rq;
+  int rc = make_request(f, pr, o, adaptive, out, &rq);
+  if (rc) return rc;
+  if (rq.kp.B == 0) return 0;  // empty ensemble: nothing to do
+  Kernel K;
+  rc = get_kernel(f, rq.spec, &K);
+  if (rc) return rc;
+  int block = rq.block ? rq.block : default_block(rq);
+  int chunk = rq.chunk ? rq.chunk : default_chunk();
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    char key[64];
+    snprintf(key, sizeof key, "%p|%lld", (void*)K.fn, (long long)(rq.kp.B >> 16));
+    auto it = g_tuned.find(key);
+    if (!rq.block && it != g_tuned.end()) { block = it->second.first; if (!rq.chunk) chunk = it->second.second; }
+  }
+  unsigned long long* work = nullptr;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (rq.spec.driver == 2) CUDA_TRY(cudaMallocAsync((void**)&work, 256, s));
+  rc = launch(rq, K, block, chunk, work, (CUstream)s);
+  if (work) cudaFreeAsync(work, s);
+  return rc;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* degpu_version(void) { return DEGPU_VERSION; }
+const char* degpu_last_error(void) { return g_err.c_str(); }
+
+int degpu_rhs_create(const char* cuda_source, int n_state, int n_param, int flags, degpu_rhs** out) {
+  if (!cuda_source || !out) return fail(DEGPU_E_INVALID, "null argument");
+  if (n_state < 1 || n_state > 32) return fail(DEGPU_E_INVALID, "state dimension must be in [1, 32]");
+  if (n_param < 0 || n_param > 64) return fail(DEGPU_E_INVALID, "parameter count must be in [0, 64]");
+  if (flags & ~(DEGPU_RHS_HAS_JAC | DEGPU_RHS_HAS_TGRAD | DEGPU_RHS_HAS_NOISE)) return fail(DEGPU_E_INVALID, "unknown flags");
+  auto* f = new degpu_rhs_s;
+  f->src = cuda_source;
+  f->N = n_state;
+  f->P = n_param;
+  f->flags = flags;
+  *out = f;
+  return 0;
+}
+
+void degpu_rhs_destroy(degpu_rhs* f) { delete f; }
+
+const char* degpu_builtin_rhs(const char* name, int* n_state, int* n_param, int* flags) {
+  if (!name) return nullptr;
+  for (int i = 0; i < degpu_embedded_nmodels; i++) {
+    if (strcmp(degpu_embedded_models[i].name, name) == 0) {
+      if (n_state) *n_state = degpu_embedded_models[i].n;
+      if (n_param) *n_param = degpu_embedded_models[i].p;
+      if (flags) *flags = degpu_embedded_models[i].flags;
+      return degpu_embedded_models[i].text;
+    }
+  }
+  return nullptr;
+}
+
+int degpu_vectorized_solve(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
+                           degpu_outputs* out, void* stream) {
+  if (opt && opt->alg == DEGPU_ALG_EM) return fail(DEGPU_E_INVALID, "GPUEM solves SDE problems: use degpu_vectorized_solve_sde");
+  return run(f, probs, opt, 0, out, stream);
+}
+
+int degpu_vectorized_asolve(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
+                            degpu_outputs* out, void* stream) {
+  return run(f, probs, opt, 1, out, stream);
+}
+
+int degpu_vectorized_solve_sde(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
+                               degpu_outputs* out, void* stream) {
+  if (opt && opt->alg != DEGPU_ALG_EM) return fail(DEGPU_E_INVALID, "SDE problems are solved with GPUEM");
+  return run(f, probs, opt, 0, out, stream);
+}
+
+int degpu_batch_solve_host(const degpu_rhs* f, const float* u0, const float* p, const void* tspan, long long B,
+                           const degpu_options* opt, int adaptive, void* ts, float* us, int L,
+                           signed char* retcode, int* naccept, int* nreject, void* stream) {
+  if (!f || !opt) return fail(DEGPU_E_INVALID, "null argument");
+  if (B < 0) return fail(DEGPU_E_INVALID, "negative trajectory count");
+  if (B == 0) return 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t tsz = opt->time_type == DEGPU_TIME_F64 ? 8 : 4;
+  const size_t n_u0 = (size_t)B * f->N * 4, n_p = (size_t)B * f->P * 4, n_tsp = (size_t)B * 2 * tsz;
+  const size_t n_ts = (size_t)B * L * tsz, n_us = (size_t)B * L * f->N * 4;
+  const size_t n_sa = opt->nsaveat ? (size_t)opt->nsaveat * (opt->saveat_per_traj ? B : 1) * tsz : 0;
+  // one device arena for inputs + outputs, freed stream-ordered at the end
+  size_t off_u0 = 0, off_p = (off_u0 + n_u0 + 255) & ~(size_t)255, off_tsp = (off_p + n_p + 255) & ~(size_t)255;
+  size_t off_sa = (off_tsp + n_tsp + 255) & ~(size_t)255, off_ts = (off_sa + n_sa + 255) & ~(size_t)255;
+  size_t off_us = (off_ts + n_ts + 255) & ~(size_t)255, off_rc = (off_us + n_us + 255) & ~(size_t)255;
+  size_t off_na = (off_rc + B + 255) & ~(size_t)255, off_nr = (off_na + 4 * B + 255) & ~(size_t)255;
+  size_t total = off_nr + 4 * B;
+  char* d = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&d, total, s));
+  int rc = 0;
+  do {
+    if (cudaMemcpyAsync(d + off_u0, u0, n_u0, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        (n_p && cudaMemcpyAsync(d + off_p, p, n_p, cudaMemcpyHostToDevice, s) != cudaSuccess) ||
+        cudaMemcpyAsync(d + off_tsp, tspan, n_tsp, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        (n_sa && cudaMemcpyAsync(d + off_sa, opt->saveat, n_sa, cudaMemcpyHostToDevice, s) != cudaSuccess)) {
+      rc = fail(DEGPU_E_CUDA, "host-to-device copy failed");
+      break;
+    }
+    degpu_problems pr{(const float*)(d + off_u0), (const float*)(d + off_p), d + off_tsp, B};
+    degpu_options o = *opt;
+    if (n_sa) o.saveat = d + off_sa;
+    degpu_outputs out{d + off_ts, (float*)(d + off_us), L, retcode ? (signed char*)(d + off_rc) : nullptr,
+                      naccept ? (int*)(d + off_na) : nullptr, nreject ? (int*)(d + off_nr) : nullptr};
+    rc = (opt->alg == DEGPU_ALG_EM) ? degpu_vectorized_solve_sde(f, &pr, &o, &out, s)
+                                    : (adaptive ? degpu_vectorized_asolve(f, &pr, &o, &out, s)
+                                                : degpu_vectorized_solve(f, &pr, &o, &out, s));
+    if (rc) break;
+    if (cudaMemcpyAsync(ts, d + off_ts, n_ts, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(us, d + off_us, n_us, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        (retcode && cudaMemcpyAsync(retcode, d + off_rc, B, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+        (naccept && cudaMemcpyAsync(naccept, d + off_na, 4 * B, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+        (nreject && cudaMemcpyAsync(nreject, d + off_nr, 4 * B, cudaMemcpyDeviceToHost, s) != cudaSuccess)) {
+      rc = fail(DEGPU_E_CUDA, "device-to-host copy failed");
+      break;
+    }
+  } while (0);
+  cudaFreeAsync(d, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (!rc && e != cudaSuccess) rc = fail(DEGPU_E_CUDA, std::string("solve failed: ") + cudaGetErrorString(e));
+  return rc;
+}
+
+int degpu_rhs_check(const degpu_rhs* f, const degpu_options* opt, int adaptive, long long* cubin_bytes) {
+  if (!f || !opt) return fail(DEGPU_E_INVALID, "null argument");
+  Request rq;
+  degpu_problems pr{nullptr, nullptr, nullptr, 0};
+  degpu_outputs out{nullptr, nullptr, opt->nsaveat ? opt->nsaveat : 2, nullptr, nullptr, nullptr};
+  degpu_options o = *opt;
+  if (!(o.dt > 0)) o.dt = 1.0;
+  if (!o.nsaveat) o.save_everystep = 0;
+  int rc = make_request(f, &pr, &o, adaptive, &out, &rq);
+  if (rc) return rc;
+  std::vector<char> cubin;
+  rc = compile_cubin(build_source(f, rq.spec), rq.spec.parity != 0, cubin);
+  if (rc) return rc;
+  if (cubin_bytes) *cubin_bytes = (long long)cubin.size();
+  return 0;
+}
+
+int degpu_kernel_info(const degpu_rhs* f, const degpu_options* opt, int adaptive, int* regs, int* local_bytes,
+                      int* max_threads) {
+  if (!f || !opt) return fail(DEGPU_E_INVALID, "null argument");
+  Request rq;
+  degpu_problems pr{nullptr, nullptr, nullptr, 0};
+  degpu_outputs out{nullptr, nullptr, opt->nsaveat ? opt->nsaveat : 2, nullptr, nullptr, nullptr};
+  degpu_options o = *opt;
+  if (!(o.dt > 0)) o.dt = 1.0;
+  int rc = make_request(f, &pr, &o, adaptive, &out, &rq);
+  if (rc) return rc;
+  Kernel K;
+  rc = get_kernel(f, rq.spec, &K);
+  if (rc) return rc;
+  if (regs) *regs = K.regs;
+  if (local_bytes) *local_bytes = K.local_bytes;
+  if (max_threads) *max_threads = K.max_threads;
+  return 0;
+}
+
+// ------------------------------------------------------------------ autotuner
+int degpu_autotune(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt, int adaptive,
+                   degpu_outputs* out, long long sample_B, void* stream, int* best_block, int* best_chunk) {
+  Request rq;
+  int rc = make_request(f, probs, opt, adaptive, out, &rq);
+  if (rc) return rc;
+  if (rq.kp.B == 0) return fail(DEGPU_E_INVALID, "cannot autotune an empty ensemble");
+  Kernel K;
+  rc = get_kernel(f, rq.spec, &K);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  Request sample = rq;
+  if (sample_B > 0 && sample_B < sample.kp.B) sample.kp.B = sample_B;
+  const int blocks[] = {64, 128, 256};
+  std::vector<int> chunks = {0};
+  if (rq.spec.driver == 2) chunks = {32, 64, 128};
+  unsigned long long* work = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&work, 256, s));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int bb = default_block(rq), bc = default_chunk();
+  for (int b : blocks) {
+    if (b > K.max_threads) continue;
+    for (int c : chunks) {
+      int cc = c ? c : default_chunk();
+      rc = launch(sample, K, b, cc, work, (CUstream)s);  // warm-up
+      if (rc) break;
+      float tot = 0.f;
+      for (int rep = 0; rep < 2 && !rc; rep++) {
+        cudaEventRecord(e0, s);
+        rc = launch(sample, K, b, cc, work, (CUstream)s);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        tot += ms;
+      }
+      if (rc) break;
+      if (tot < best) { best = tot; bb = b; bc = cc; }
+    }
+    if (rc) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(work, s);
+  if (rc) return rc;
+  CUDA_TRY(cudaStreamSynchronize(s));
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    char key[64];
+    snprintf(key, sizeof key, "%p|%lld", (void*)K.fn, (long long)(rq.kp.B >> 16));
+    g_tuned[key] = {bb, bc};
+  }
+  if (best_block) *best_block = bb;
+  if (best_chunk) *best_chunk = bc;
+  return 0;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ plans (CUDA graphs)
+struct degpu_plan_s {
+  Request rq;
+  Kernel K;
+  int block = 0, chunk = 0, grid = 0;
+  unsigned long long* work = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+int degpu_plan_create(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt, int adaptive,
+                      degpu_outputs* out, void* stream, degpu_plan** plan) {
+  if (!plan) return fail(DEGPU_E_INVALID, "null plan");
+  std::unique_ptr<degpu_plan_s> pl(new degpu_plan_s);
+  int rc = make_request(f, probs, opt, adaptive, out, &pl->rq);
+  if (rc) return rc;
+  if (pl->rq.kp.B == 0) return fail(DEGPU_E_INVALID, "cannot plan an empty ensemble");
+  rc = get_kernel(f, pl->rq.spec, &pl->K);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  pl->block = opt->block;
+  pl->chunk = opt->chunk;
+  if (!pl->block) {
+    long long sample = std::min<long long>(pl->rq.kp.B, 1LL << 18);
+    rc = degpu_autotune(f, probs, opt, adaptive, out, sample, stream, &pl->block, &pl->chunk);
+    if (rc) return rc;
+  }
+  if (!pl->chunk) pl->chunk = default_chunk();
+  CUDA_TRY(cudaMalloc((void**)&pl->work, 256));
+  pl->grid = grid_for(pl->rq, pl->K, pl->block);
+  cudaStream_t cap;
+  CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+  rc = launch(pl->rq, pl->K, pl->block, pl->chunk, pl->work, (CUstream)cap);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(cap, &g);
+  cudaStreamDestroy(cap);
+  if (rc) { if (g) cudaGraphDestroy(g); cudaFree(pl->work); return rc; }
+  if (e != cudaSuccess) { cudaFree(pl->work); return fail(DEGPU_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e)); }
+  pl->graph = g;
+  e = cudaGraphInstantiate(&pl->exec, g, 0);
+  if (e != cudaSuccess) { cudaGraphDestroy(g); cudaFree(pl->work); return fail(DEGPU_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
+  (void)s;
+  *plan = pl.release();
+  return 0;
+}
+
+int degpu_plan_launch(degpu_plan* plan, void* stream) {
+  if (!plan) return fail(DEGPU_E_INVALID, "null plan");
+  CUDA_TRY(cudaGraphLaunch(plan->exec, (cudaStream_t)stream));
+  return 0;
+}
+
+int degpu_plan_info(const degpu_plan* plan, int* block, int* chunk, int* grid, int* driver, int* regs) {
+  if (!plan) return fail(DEGPU_E_INVALID, "null plan");
+  if (block) *block = plan->block;
+  if (chunk) *chunk = plan->chunk;
+  if (grid) *grid = plan->grid;
+  if (driver) *driver = plan->rq.spec.driver;
+  if (regs) *regs = plan->K.regs;
+  return 0;
+}
+
+void degpu_plan_destroy(degpu_plan* plan) {
+  if (!plan) return;
+  if (plan->exec) cudaGraphExecDestroy(plan->exec);
+  if (plan->graph) cudaGraphDestroy(plan->graph);
+  if (plan->work) cudaFree(plan->work);
+  delete plan;
+}
+
+}  // extern "C"

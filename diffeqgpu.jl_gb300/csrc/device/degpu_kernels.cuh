@@ -1,0 +1,977 @@
+// Ensemble ODE/SDE kernels for sm_103a: one trajectory per thread, state and stage
+// vectors in registers, method coefficients in constant memory.
+//
+// This header is compiled by NVRTC after the user's right-hand side.  The host library
+// defines, per translation unit:
+//   DEGPU_N, DEGPU_P        state / parameter dimensions
+//   DEGPU_TT                time type (float: the reference's Float32 tspan; double: FP64 time)
+//   DEGPU_ALG               0 Tsit5, 1 Vern7, 2 Rosenbrock23, 3 Rodas5P, 4 EM
+//   DEGPU_DRIVER            0 fixed step, 1 adaptive (one trajectory per thread),
+//                           2 adaptive persistent (warp refill + work stealing), 3 EM
+//   DEGPU_PARITY            1: no FMA (set by --fmad=false), portable pow, Cramer solves
+//   DEGPU_JAC, DEGPU_TGRAD  0 forward-mode AD, 1 user function, 2 finite differences
+//   DEGPU_LINSOLVE_REFINE   fast mode: 1 = one compensated (double-float) residual refinement
+// The reference's semantics (file:line in DiffEqGPU.jl) are cited at each piece.
+#pragma once
+#include "tableaus_gen.cuh"
+
+#ifndef DEGPU_N
+#error "DEGPU_N must be defined"
+#endif
+
+namespace degpu {
+
+typedef DEGPU_TT Tt;
+constexpr int N = DEGPU_N;
+constexpr int NP = DEGPU_P > 0 ? DEGPU_P : 1;
+
+#if DEGPU_ALG == 0
+constexpr int NK = 7;
+constexpr int ORDER = 5;
+#elif DEGPU_ALG == 1
+constexpr int NK = 10;
+constexpr int ORDER = 7;
+#elif DEGPU_ALG == 2
+constexpr int NK = 2;
+constexpr int ORDER = 2;
+#elif DEGPU_ALG == 3
+constexpr int NK = 3;
+constexpr int ORDER = 5;
+#else
+constexpr int NK = 1;
+constexpr int ORDER = 1;
+#endif
+
+// ------------------------------------------------------------------ Tsit5 coefficients
+// Tsitouras (2011) 5(4) pair and its dense output, as SimpleDiffEq 1.11 builds them
+// (_build_atsit5_caches / bθs; used at nonstiff/types.jl:326, 359 and
+// nonstiff/interpolants.jl:379).  FP32 values of the published FP64 coefficients.
+enum {
+  TS_c1, TS_c2, TS_c3, TS_c4,
+  TS_a21, TS_a31, TS_a32, TS_a41, TS_a42, TS_a43, TS_a51, TS_a52, TS_a53, TS_a54,
+  TS_a61, TS_a62, TS_a63, TS_a64, TS_a65, TS_a71, TS_a72, TS_a73, TS_a74, TS_a75, TS_a76,
+  TS_bt1, TS_bt2, TS_bt3, TS_bt4, TS_bt5, TS_bt6, TS_bt7,
+  TS_r11, TS_r12, TS_r13, TS_r14, TS_r22, TS_r23, TS_r24, TS_r32, TS_r33, TS_r34,
+  TS_r42, TS_r43, TS_r44, TS_r52, TS_r53, TS_r54, TS_r62, TS_r63, TS_r64, TS_r72, TS_r73, TS_r74,
+  TS_COUNT
+};
+__constant__ float c_tsit5[TS_COUNT] = {
+  (float)0.161, (float)0.327, (float)0.9, (float)0.9800255409045097,
+  (float)0.161, (float)-0.008480655492356989, (float)0.335480655492357,
+  (float)2.897153057105493, (float)-6.359448489975075, (float)4.3622954328695815,
+  (float)5.325864828439257, (float)-11.748883564062828, (float)7.4955393428898365, (float)-0.09249506636175525,
+  (float)5.86145544294642, (float)-12.92096931784711, (float)8.159367898576159, (float)-0.071584973281401, (float)-0.028269050394068383,
+  (float)0.09646076681806523, (float)0.01, (float)0.4798896504144996, (float)1.379008574103742, (float)-3.290069515436081, (float)2.324710524099774,
+  (float)-0.00178001105222577714, (float)-0.0008164344596567469, (float)0.007880878010261995, (float)-0.1447110071732629,
+  (float)0.5823571654525552, (float)-0.45808210592918697, (float)0.015151515151515152,
+  1.0f, (float)-2.763706197274826, (float)2.9132554618219126, (float)-1.0530884977290216,
+  (float)0.13169999999999998, (float)-0.2234, (float)0.1017,
+  (float)3.9302962368947516, (float)-5.941033872131505, (float)2.490627285651253,
+  (float)-12.411077166933676, (float)30.33818863028232, (float)-16.548102889244902,
+  (float)37.50931341651104, (float)-88.1789048947664, (float)47.37952196281928,
+  (float)-27.896526289197286, (float)65.09189467479366, (float)-34.87065786149661,
+  1.5f, -4.0f, 2.5f,
+};
+#define TS(n) c_tsit5[TS_##n]
+#define V7(n) c_vern7[VERN7_##n]
+#define V7X(n) c_vern7x[VERN7X_##n]
+#define V7I(n) c_vern7i[VERN7I_##n]
+#define RP(n) c_rodas5p[RODAS5P_##n]
+
+// ------------------------------------------------------------------ small helpers
+DEGPU_DEV float tstage(Tt t, float c, float dt) { return (float)(t + (Tt)(c * dt)); }
+
+DEGPU_DEV float ctrl_pow(float x, float y) {
+#if DEGPU_PARITY
+  return pm_powf(x, y);
+#else
+  return x == 0.0f ? 0.0f : __powf(x, y);
+#endif
+}
+
+DEGPU_DEV void rhs(float* du, const float* u, const float* p, float t) { degpu_f<float>(du, u, p, t); }
+
+// DiffEqBase.ODE_DEFAULT_NORM on a static vector: sqrt(sum(abs2, x) / length(x))
+DEGPU_DEV float scaled_norm(const float* e, const float* up, const float* u, float abstol, float reltol) {
+  float s = 0.0f;
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    float w = e[i] / (abstol + jl_max(fabsf(up[i]), fabsf(u[i])) * reltol);
+    s = (i == 0) ? w * w : s + w * w;
+  }
+  return sqrtf(s / (float)N);
+}
+
+// ------------------------------------------------------------------ Jacobian / tgrad
+// build_J_W / build_tgrad (nlsolve/type.jl:129-157): user function, else forward-mode
+// AD, else finite differences with dx = sqrt(eps(Float32)) (alg_utils.jl:17-27).
+DEGPU_DEV void jacobian(float* J, const float* u, const float* p, float t) {
+#if DEGPU_JAC == 1
+  degpu_jac(J, u, p, t);
+#elif DEGPU_JAC == 2
+  const float dx = 3.45266983e-04f;  // sqrt(eps(Float32))
+  float f0[N], f1[N], x[N];
+  rhs(f0, u, p, t);
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+#pragma unroll
+    for (int i = 0; i < N; i++) x[i] = u[i];
+    x[j] = x[j] + dx;
+    rhs(f1, x, p, t);
+#pragma unroll
+    for (int i = 0; i < N; i++) J[i + N * j] = (f1[i] - f0[i]) / dx;
+  }
+#else
+  Dual<N> ud[N], fd[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) { ud[i] = Dual<N>(u[i]); ud[i].d[i] = 1.0f; }
+  degpu_f<Dual<N>>(fd, ud, p, Dual<N>(t));
+#pragma unroll
+  for (int j = 0; j < N; j++)
+#pragma unroll
+    for (int i = 0; i < N; i++) J[i + N * j] = fd[i].d[j];
+#endif
+}
+DEGPU_DEV void tgrad(float* dT, const float* u, const float* p, float t) {
+#if DEGPU_TGRAD == 1
+  degpu_tgrad(dT, u, p, t);
+#elif DEGPU_TGRAD == 2
+  const float h = 3.45266983e-04f;
+  float f0[N], f1[N];
+  rhs(f1, u, p, t + h);
+  rhs(f0, u, p, t);
+#pragma unroll
+  for (int i = 0; i < N; i++) dT[i] = (f1[i] - f0[i]) / h;
+#else
+  Dual<1> ud[N], fd[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) ud[i] = Dual<1>(u[i]);
+  Dual<1> td(t);
+  td.d[0] = 1.0f;
+  degpu_f<Dual<1>>(fd, ud, p, td);
+#pragma unroll
+  for (int i = 0; i < N; i++) dT[i] = fd[i].d[0];
+#endif
+}
+
+// ------------------------------------------------------------------ linear solves
+#define A_(i, j) a[(i - 1) + N * (j - 1)]
+#if DEGPU_PARITY || DEGPU_N > 3
+// linear_solve (linalg/linsolve.jl:8-57): N<=3 by Cramer's rule with StaticArrays' det
+// (triple product), recomputed for every right-hand side like the reference; larger N by
+// partial-pivot LU.  Parity mode keeps exactly this arithmetic.
+DEGPU_DEV void solve_cramer_or_lu(const float* a, const float* b, float* x) {
+  if constexpr (N == 1) {
+    x[0] = b[0] / a[0];
+  } else if constexpr (N == 2) {
+    float d = a[0] * a[3] - a[2] * a[1];
+    x[0] = (A_(2, 2) * b[0] - A_(1, 2) * b[1]) / d;
+    x[1] = (A_(1, 1) * b[1] - A_(2, 1) * b[0]) / d;
+  } else if constexpr (N == 3) {
+    float c0 = a[4] * a[8] - a[5] * a[7], c1 = a[5] * a[6] - a[3] * a[8], c2 = a[3] * a[7] - a[4] * a[6];
+    float d = a[0] * c0 + a[1] * c1 + a[2] * c2;
+    x[0] = ((A_(2, 2) * A_(3, 3) - A_(2, 3) * A_(3, 2)) * b[0] + (A_(1, 3) * A_(3, 2) - A_(1, 2) * A_(3, 3)) * b[1] + (A_(1, 2) * A_(2, 3) - A_(1, 3) * A_(2, 2)) * b[2]) / d;
+    x[1] = ((A_(2, 3) * A_(3, 1) - A_(2, 1) * A_(3, 3)) * b[0] + (A_(1, 1) * A_(3, 3) - A_(1, 3) * A_(3, 1)) * b[1] + (A_(1, 3) * A_(2, 1) - A_(1, 1) * A_(2, 3)) * b[2]) / d;
+    x[2] = ((A_(2, 1) * A_(3, 2) - A_(2, 2) * A_(3, 1)) * b[0] + (A_(1, 2) * A_(3, 1) - A_(1, 1) * A_(3, 2)) * b[1] + (A_(1, 1) * A_(2, 2) - A_(1, 2) * A_(2, 1)) * b[2]) / d;
+  } else {
+    float LU[N][N], y[N];
+    int piv[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      piv[i] = i;
+#pragma unroll
+      for (int j = 0; j < N; j++) LU[i][j] = a[i + N * j];
+    }
+    for (int kk = 0; kk < N; kk++) {
+      int pr = kk;
+      float best = fabsf(LU[kk][kk]);
+      for (int i = kk + 1; i < N; i++)
+        if (fabsf(LU[i][kk]) > best) { best = fabsf(LU[i][kk]); pr = i; }
+      if (pr != kk) {
+        for (int j = 0; j < N; j++) { float t = LU[kk][j]; LU[kk][j] = LU[pr][j]; LU[pr][j] = t; }
+        int t = piv[kk]; piv[kk] = piv[pr]; piv[pr] = t;
+      }
+      for (int i = kk + 1; i < N; i++) {
+        LU[i][kk] = LU[i][kk] / LU[kk][kk];
+        for (int j = kk + 1; j < N; j++) LU[i][j] = LU[i][j] - LU[i][kk] * LU[kk][j];
+      }
+    }
+    for (int i = 0; i < N; i++) {
+      float s = b[piv[i]];
+      for (int j = 0; j < i; j++) s = s - LU[i][j] * y[j];
+      y[i] = s;
+    }
+    for (int i = N - 1; i >= 0; i--) {
+      float s = y[i];
+      for (int j = i + 1; j < N; j++) s = s - LU[i][j] * x[j];
+      x[i] = s / LU[i][i];
+    }
+  }
+}
+#endif
+#undef A_
+
+// Fast mode: factor W once per attempt (partial pivoting, fully unrolled), reuse the
+// factors for every stage solve, then one refinement step whose residual b - W x is
+// accumulated in double-float arithmetic (error-free FMA products + two-sum), i.e. to
+// ~48 significant bits on the FP32 pipes.  GB300's FP64 rate is a small fraction of its
+// FP32 rate, so this is the FP64-class residual at FP32 cost.
+struct LinSys {
+  float W[N * N];   // original matrix (column-major) for the residual
+  float LU[N * N];  // row-permuted LU factors, column-major, unit lower
+  int piv[N];
+  DEGPU_DEV void factor() {
+#pragma unroll
+    for (int i = 0; i < N * N; i++) LU[i] = W[i];
+#pragma unroll
+    for (int i = 0; i < N; i++) piv[i] = i;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      int pr = k;
+      float best = fabsf(LU[k + N * k]);
+#pragma unroll
+      for (int i = k + 1; i < N; i++) {
+        float v = fabsf(LU[i + N * k]);
+        if (v > best) { best = v; pr = i; }
+      }
+      // swap rows k and pr with predicated selects (keeps every index compile-time)
+#pragma unroll
+      for (int i = k + 1; i < N; i++) {
+        bool sw = (i == pr);
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+          float a = LU[k + N * j], b = LU[i + N * j];
+          LU[k + N * j] = sw ? b : a;
+          LU[i + N * j] = sw ? a : b;
+        }
+        int pa = piv[k], pb = piv[i];
+        piv[k] = sw ? pb : pa;
+        piv[i] = sw ? pa : pb;
+      }
+      float inv = 1.0f / LU[k + N * k];
+#pragma unroll
+      for (int i = k + 1; i < N; i++) {
+        LU[i + N * k] = LU[i + N * k] * inv;
+#pragma unroll
+        for (int j = k + 1; j < N; j++) LU[i + N * j] = LU[i + N * j] - LU[i + N * k] * LU[k + N * j];
+      }
+    }
+  }
+  DEGPU_DEV void lusolve(const float* b, float* x) const {
+    float y[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      float s = 0.0f;
+#pragma unroll
+      for (int j = 0; j < N; j++) s = (piv[i] == j) ? b[j] : s;
+#pragma unroll
+      for (int j = 0; j < i; j++) s = s - LU[i + N * j] * y[j];
+      y[i] = s;
+    }
+#pragma unroll
+    for (int i = N - 1; i >= 0; i--) {
+      float s = y[i];
+#pragma unroll
+      for (int j = i + 1; j < N; j++) s = s - LU[i + N * j] * x[j];
+      x[i] = s / LU[i + N * i];
+    }
+  }
+  DEGPU_DEV void solve(const float* b, float* x) const {
+#if DEGPU_PARITY || DEGPU_N > 3
+    solve_cramer_or_lu(W, b, x);
+#else
+    lusolve(b, x);
+#if DEGPU_LINSOLVE_REFINE
+    float r[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      // r_i = b_i - sum_j W_ij x_j with hi/lo accumulation (TwoProduct via fmaf, TwoSum)
+      float hi = b[i], lo = 0.0f;
+#pragma unroll
+      for (int j = 0; j < N; j++) {
+        float pr = -W[i + N * j] * x[j];
+        float pe = fmaf(-W[i + N * j], x[j], -pr);
+        float s = hi + pr;
+        float bb = s - hi;
+        float e = (hi - (s - bb)) + (pr - bb);
+        hi = s;
+        lo = lo + (e + pe);
+      }
+      r[i] = hi + lo;
+    }
+    float dx[N];
+    lusolve(r, dx);
+#pragma unroll
+    for (int i = 0; i < N; i++) x[i] = x[i] + dx[i];
+#endif
+#endif
+  }
+};
+
+// ------------------------------------------------------------------ per-lane integrator
+// The fields of the reference's GPU*Integrator structs (integrators/*/types.jl) that the
+// kernel path reads, kept in registers.
+struct Lane {
+  float u[N], uprev[N];
+  float k[NK][N];
+#if DEGPU_ALG == 2 || DEGPU_ALG == 3
+  float J[N * N], dT[N];
+#endif
+#if DEGPU_ALG == 2
+  float F0[N];
+#endif
+  float p[NP];
+  Tt t, tprev, tf, t0;
+  float dt, dtnew, qold, abstol, reltol;
+  int cur_t, step_idx, nattempt, naccept, nreject, status;
+  bool need_begin, fsal;
+};
+
+// ------------------------------------------------------------------ Tsit5 (gpu_tsit5_perform_step.jl)
+#if DEGPU_ALG == 0
+DEGPU_DEV void begin_step(Lane& L) {
+  // FSAL: k1 = k7 of the previous step unless u was modified (:29-34, :92-97)
+  if (!L.fsal) { rhs(L.k[0], L.uprev, L.p, (float)L.t); L.fsal = true; }
+  else {
+#pragma unroll
+    for (int i = 0; i < N; i++) L.k[0][i] = L.k[6][i];
+  }
+}
+template <bool ADAPTIVE>
+DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
+  float tmp[N];
+  const float* up = L.uprev;
+  float(*k)[N] = L.k;
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + (dt * TS(a21)) * k[0][i];
+  rhs(k[1], tmp, L.p, tstage(t, TS(c1), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (TS(a31) * k[0][i] + TS(a32) * k[1][i]);
+  rhs(k[2], tmp, L.p, tstage(t, TS(c2), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (TS(a41) * k[0][i] + TS(a42) * k[1][i] + TS(a43) * k[2][i]);
+  rhs(k[3], tmp, L.p, tstage(t, TS(c3), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (TS(a51) * k[0][i] + TS(a52) * k[1][i] + TS(a53) * k[2][i] + TS(a54) * k[3][i]);
+  rhs(k[4], tmp, L.p, tstage(t, TS(c4), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (TS(a61) * k[0][i] + TS(a62) * k[1][i] + TS(a63) * k[2][i] + TS(a64) * k[3][i] + TS(a65) * k[4][i]);
+  rhs(k[5], tmp, L.p, (float)(t + (Tt)dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    if (ADAPTIVE)  // :114
+      u[i] = up[i] + dt * (TS(a71) * k[0][i] + TS(a72) * k[1][i] + TS(a73) * k[2][i] + TS(a74) * k[3][i] + TS(a75) * k[4][i] + TS(a76) * k[5][i]);
+    else  // :47-48
+      u[i] = up[i] + dt * ((TS(a71) * k[0][i] + TS(a72) * k[1][i] + TS(a73) * k[2][i] + TS(a74) * k[3][i]) + TS(a75) * k[4][i] + TS(a76) * k[5][i]);
+  }
+  rhs(k[6], u, L.p, (float)(t + (Tt)dt));
+  if (ADAPTIVE) {
+#pragma unroll
+    for (int i = 0; i < N; i++)
+      err[i] = dt * (TS(bt1) * k[0][i] + TS(bt2) * k[1][i] + TS(bt3) * k[2][i] + TS(bt4) * k[3][i] + TS(bt5) * k[4][i] + TS(bt6) * k[5][i] + TS(bt7) * k[6][i]);
+  }
+}
+// nonstiff/interpolants.jl:372-387 with SimpleDiffEq.bθs (Horner)
+DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
+  float b0 = (((TS(r14) * th + TS(r13)) * th + TS(r12)) * th + TS(r11)) * th;
+  float b1 = (((TS(r24) * th + TS(r23)) * th + TS(r22)) * th) * th;
+  float b2 = (((TS(r34) * th + TS(r33)) * th + TS(r32)) * th) * th;
+  float b3 = (((TS(r44) * th + TS(r43)) * th + TS(r42)) * th) * th;
+  float b4 = (((TS(r54) * th + TS(r53)) * th + TS(r52)) * th) * th;
+  float b5 = (((TS(r64) * th + TS(r63)) * th + TS(r62)) * th) * th;
+  float b6 = (((TS(r74) * th + TS(r73)) * th + TS(r72)) * th) * th;
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    out[i] = L.uprev[i] + dt * (b0 * L.k[0][i] + b1 * L.k[1][i] + b2 * L.k[2][i] + b3 * L.k[3][i] + b4 * L.k[4][i] + b5 * L.k[5][i] + b6 * L.k[6][i]);
+}
+#endif
+
+// ------------------------------------------------------------------ Vern7 (gpu_vern7_perform_step.jl)
+#if DEGPU_ALG == 1
+DEGPU_DEV void begin_step(Lane& L) {
+  // not FSAL: k1 = f(uprev, p, t) every step (:30, :117; one evaluation per step suffices)
+  rhs(L.k[0], L.uprev, L.p, (float)L.t);
+}
+template <bool ADAPTIVE>
+DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
+  float tmp[N];
+  const float* up = L.uprev;
+  float(*k)[N] = L.k;
+  float a = dt * V7(a021);
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + a * k[0][i];
+  rhs(k[1], tmp, L.p, tstage(t, V7(c2), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7(a031) * k[0][i] + V7(a032) * k[1][i]);
+  rhs(k[2], tmp, L.p, tstage(t, V7(c3), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7(a041) * k[0][i] + V7(a043) * k[2][i]);
+  rhs(k[3], tmp, L.p, tstage(t, V7(c4), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7(a051) * k[0][i] + V7(a053) * k[2][i] + V7(a054) * k[3][i]);
+  rhs(k[4], tmp, L.p, tstage(t, V7(c5), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7(a061) * k[0][i] + V7(a063) * k[2][i] + V7(a064) * k[3][i] + V7(a065) * k[4][i]);
+  rhs(k[5], tmp, L.p, tstage(t, V7(c6), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7(a071) * k[0][i] + V7(a073) * k[2][i] + V7(a074) * k[3][i] + V7(a075) * k[4][i] + V7(a076) * k[5][i]);
+  rhs(k[6], tmp, L.p, tstage(t, V7(c7), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7(a081) * k[0][i] + V7(a083) * k[2][i] + V7(a084) * k[3][i] + V7(a085) * k[4][i] + V7(a086) * k[5][i] + V7(a087) * k[6][i]);
+  rhs(k[7], tmp, L.p, tstage(t, V7(c8), dt));
+  float g10[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    tmp[i] = up[i] + dt * (V7(a091) * k[0][i] + V7(a093) * k[2][i] + V7(a094) * k[3][i] + V7(a095) * k[4][i] + V7(a096) * k[5][i] + V7(a097) * k[6][i] + V7(a098) * k[7][i]);
+    g10[i] = up[i] + dt * (V7(a101) * k[0][i] + V7(a103) * k[2][i] + V7(a104) * k[3][i] + V7(a105) * k[4][i] + V7(a106) * k[5][i] + V7(a107) * k[6][i]);
+  }
+  rhs(k[8], tmp, L.p, (float)(t + (Tt)dt));
+  rhs(k[9], g10, L.p, (float)(t + (Tt)dt));
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    u[i] = up[i] + dt * (V7(b1) * k[0][i] + V7(b4) * k[3][i] + V7(b5) * k[4][i] + V7(b6) * k[5][i] + V7(b7) * k[6][i] + V7(b8) * k[7][i] + V7(b9) * k[8][i]);
+  if (ADAPTIVE) {
+#pragma unroll
+    for (int i = 0; i < N; i++)
+      err[i] = dt * (V7(btilde1) * k[0][i] + V7(btilde4) * k[3][i] + V7(btilde5) * k[4][i] + V7(btilde6) * k[5][i] + V7(btilde7) * k[6][i] + V7(btilde8) * k[7][i] + V7(btilde9) * k[8][i] + V7(btilde10) * k[9][i]);
+  }
+}
+DEGPU_DEV float horner6(float th, float a0, float a1, float a2, float a3, float a4, float a5) {
+  return ((((a5 * th + a4) * th + a3) * th + a2) * th + a1) * th + a0;
+}
+// nonstiff/interpolants.jl:28-190: tail-sum q_i(Θ) + 6 extra stages
+DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
+  float q[13];
+#define SYN(II, OUT)                                                                        \
+  {                                                                                         \
+    float s5 = V7I(r##II##7), s4 = V7I(r##II##6) + s5, s3 = V7I(r##II##5) + s4;             \
+    float s2 = V7I(r##II##4) + s3, s1 = V7I(r##II##3) + s2;                                 \
+    OUT = horner6(th, V7I(r##II##2) + s1, s1, s2, s3, s4, s5);                              \
+  }
+  {
+    float s15 = V7I(r017), s14 = V7I(r016) + s15, s13 = V7I(r015) + s14, s12 = V7I(r014) + s13;
+    float s11 = V7I(r013) + s12, s10 = V7I(r012) + s11;
+    q[0] = horner6(th, s10, s11, s12, s13, s14, s15);
+  }
+  SYN(04, q[1]) SYN(05, q[2]) SYN(06, q[3]) SYN(07, q[4]) SYN(08, q[5]) SYN(09, q[6])
+  SYN(11, q[7]) SYN(12, q[8]) SYN(13, q[9]) SYN(14, q[10]) SYN(15, q[11]) SYN(16, q[12])
+#undef SYN
+  const float* up = L.uprev;
+  const float(*k)[N] = L.k;
+  float k11[N], k12[N], k13[N], k14[N], k15[N], k16[N], tmp[N];
+  Tt tp = L.tprev;
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7X(a1101) * k[0][i] + V7X(a1104) * k[3][i] + V7X(a1105) * k[4][i] + V7X(a1106) * k[5][i] + V7X(a1107) * k[6][i] + V7X(a1108) * k[7][i] + V7X(a1109) * k[8][i]);
+  rhs(k11, tmp, L.p, tstage(tp, V7X(c11), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7X(a1201) * k[0][i] + V7X(a1204) * k[3][i] + V7X(a1205) * k[4][i] + V7X(a1206) * k[5][i] + V7X(a1207) * k[6][i] + V7X(a1208) * k[7][i] + V7X(a1209) * k[8][i] + V7X(a1211) * k11[i]);
+  rhs(k12, tmp, L.p, tstage(tp, V7X(c12), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7X(a1301) * k[0][i] + V7X(a1304) * k[3][i] + V7X(a1305) * k[4][i] + V7X(a1306) * k[5][i] + V7X(a1307) * k[6][i] + V7X(a1308) * k[7][i] + V7X(a1309) * k[8][i] + V7X(a1311) * k11[i] + V7X(a1312) * k12[i]);
+  rhs(k13, tmp, L.p, tstage(tp, V7X(c13), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7X(a1401) * k[0][i] + V7X(a1404) * k[3][i] + V7X(a1405) * k[4][i] + V7X(a1406) * k[5][i] + V7X(a1407) * k[6][i] + V7X(a1408) * k[7][i] + V7X(a1409) * k[8][i] + V7X(a1411) * k11[i] + V7X(a1412) * k12[i] + V7X(a1413) * k13[i]);
+  rhs(k14, tmp, L.p, tstage(tp, V7X(c14), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7X(a1501) * k[0][i] + V7X(a1504) * k[3][i] + V7X(a1505) * k[4][i] + V7X(a1506) * k[5][i] + V7X(a1507) * k[6][i] + V7X(a1508) * k[7][i] + V7X(a1509) * k[8][i] + V7X(a1511) * k11[i] + V7X(a1512) * k12[i] + V7X(a1513) * k13[i]);
+  rhs(k15, tmp, L.p, tstage(tp, V7X(c15), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7X(a1601) * k[0][i] + V7X(a1604) * k[3][i] + V7X(a1605) * k[4][i] + V7X(a1606) * k[5][i] + V7X(a1607) * k[6][i] + V7X(a1608) * k[7][i] + V7X(a1609) * k[8][i] + V7X(a1611) * k11[i] + V7X(a1612) * k12[i] + V7X(a1613) * k13[i]);
+  rhs(k16, tmp, L.p, tstage(tp, V7X(c16), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    float step_sum = dt * (V7(b1) * k[0][i] + V7(b4) * k[3][i] + V7(b5) * k[4][i] + V7(b6) * k[5][i] + V7(b7) * k[6][i] + V7(b8) * k[7][i] + V7(b9) * k[8][i]);
+    float corr = dt * (k[0][i] * q[0] + k[3][i] * q[1] + k[4][i] * q[2] + k[5][i] * q[3] + k[6][i] * q[4] + k[7][i] * q[5] + k[8][i] * q[6] +
+                       k11[i] * q[7] + k12[i] * q[8] + k13[i] * q[9] + k14[i] * q[10] + k15[i] * q[11] + k16[i] * q[12]);
+    out[i] = up[i] + th * step_sum + th * (th - 1.0f) * corr;
+  }
+}
+#endif
+
+// ------------------------------------------------------------------ Rosenbrock23 (gpu_rosenbrock23_perform_step.jl)
+#if DEGPU_ALG == 2
+DEGPU_DEV void begin_step(Lane& L) {
+  // J, dT and F0 = f(uprev, t) depend only on (uprev, t): once per step (:38-49, :114-124)
+  float tf_ = (float)L.t;
+  jacobian(L.J, L.uprev, L.p, tf_);
+  tgrad(L.dT, L.uprev, L.p, tf_);
+  rhs(L.F0, L.uprev, L.p, tf_);
+}
+template <bool ADAPTIVE>
+DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
+  const float d = 1.0f / (2.0f + sqrtf(2.0f));
+  float gam = dt * d, dto2 = dt / 2.0f, dto6 = dt / 6.0f;
+  LinSys S;
+#pragma unroll
+  for (int j = 0; j < N; j++)
+#pragma unroll
+    for (int i = 0; i < N; i++) S.W[i + N * j] = (i == j ? 1.0f : 0.0f) - gam * L.J[i + N * j];
+#if !(DEGPU_PARITY || DEGPU_N > 3)
+  S.factor();
+#endif
+  float rhsv[N], tmp[N], F1[N];
+  float* k1 = L.k[0];
+  float* k2 = L.k[1];
+#pragma unroll
+  for (int i = 0; i < N; i++) rhsv[i] = L.F0[i] + gam * L.dT[i];
+  S.solve(rhsv, k1);
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = L.uprev[i] + dto2 * k1[i];
+  rhs(F1, tmp, L.p, (float)(t + (Tt)dto2));
+#pragma unroll
+  for (int i = 0; i < N; i++) rhsv[i] = F1[i] - k1[i];
+  S.solve(rhsv, k2);
+#pragma unroll
+  for (int i = 0; i < N; i++) { k2[i] = k2[i] + k1[i]; u[i] = L.uprev[i] + dt * k2[i]; }
+  if (ADAPTIVE) {
+    const float e32 = 6.0f + sqrtf(2.0f);
+    float F2[N], k3[N];
+    rhs(F2, u, L.p, (float)(t + (Tt)dt));
+#pragma unroll
+    for (int i = 0; i < N; i++) rhsv[i] = F2[i] - e32 * (k2[i] - F1[i]) - 2.0f * (k1[i] - L.F0[i]) + dt * L.dT[i];
+    S.solve(rhsv, k3);
+#pragma unroll
+    for (int i = 0; i < N; i++) err[i] = dto6 * (k1[i] - 2.0f * k2[i] + k3[i]);
+  }
+}
+// nonstiff/interpolants.jl:389-399
+DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
+  const float d = 1.0f / (2.0f + sqrtf(2.0f));
+  float c1 = th * (1.0f - th) / (1.0f - 2.0f * d);
+  float c2 = th * (th - 2.0f * d) / (1.0f - 2.0f * d);
+#pragma unroll
+  for (int i = 0; i < N; i++) out[i] = L.uprev[i] + dt * (c1 * L.k[0][i] + c2 * L.k[1][i]);
+}
+#endif
+
+// ------------------------------------------------------------------ Rodas5P (gpu_rodas5P_perform_step.jl)
+#if DEGPU_ALG == 3
+DEGPU_DEV void begin_step(Lane& L) {
+  float tf_ = (float)L.t;  // J, dT once per step, outside the reject loop (:182-186)
+  jacobian(L.J, L.uprev, L.p, tf_);
+  tgrad(L.dT, L.uprev, L.p, tf_);
+}
+template <bool ADAPTIVE>
+DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* uout, float* err) {
+  const float* up = L.uprev;
+  float dtC21 = RP(C21) / dt, dtC31 = RP(C31) / dt, dtC32 = RP(C32) / dt, dtC41 = RP(C41) / dt, dtC42 = RP(C42) / dt, dtC43 = RP(C43) / dt;
+  float dtC51 = RP(C51) / dt, dtC52 = RP(C52) / dt, dtC53 = RP(C53) / dt, dtC54 = RP(C54) / dt;
+  float dtC61 = RP(C61) / dt, dtC62 = RP(C62) / dt, dtC63 = RP(C63) / dt, dtC64 = RP(C64) / dt, dtC65 = RP(C65) / dt;
+  float dtC71 = RP(C71) / dt, dtC72 = RP(C72) / dt, dtC73 = RP(C73) / dt, dtC74 = RP(C74) / dt, dtC75 = RP(C75) / dt, dtC76 = RP(C76) / dt;
+  float dtC81 = RP(C81) / dt, dtC82 = RP(C82) / dt, dtC83 = RP(C83) / dt, dtC84 = RP(C84) / dt, dtC85 = RP(C85) / dt, dtC86 = RP(C86) / dt, dtC87 = RP(C87) / dt;
+  float dtd1 = dt * RP(d1), dtd2 = dt * RP(d2), dtd3 = dt * RP(d3), dtd4 = dt * RP(d4), dtd5 = dt * RP(d5);
+  float dtgamma = dt * RP(gamma);
+  float inv_dtg = 1.0f / dtgamma;
+  LinSys S;
+#pragma unroll
+  for (int j = 0; j < N; j++)
+#pragma unroll
+    for (int i = 0; i < N; i++) S.W[i + N * j] = L.J[i + N * j] - (i == j ? 1.0f : 0.0f) * inv_dtg;
+#if !(DEGPU_PARITY || DEGPU_N > 3)
+  S.factor();
+#endif
+  float du[N], u[N], lt[N];
+  float k1[N], k2[N], k3[N], k4[N], k5[N], k6[N], k7[N], k8[N];
+#define SOLVE(K)                                  \
+  {                                               \
+    _Pragma("unroll") for (int i = 0; i < N; i++) lt[i] = -lt[i]; \
+    S.solve(lt, K);                               \
+  }
+  rhs(du, up, L.p, (float)t);
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd1 * L.dT[i];
+  SOLVE(k1);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + RP(a21) * k1[i];
+  rhs(du, u, L.p, tstage(t, RP(c2), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd2 * L.dT[i] + dtC21 * k1[i];
+  SOLVE(k2);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + RP(a31) * k1[i] + RP(a32) * k2[i];
+  rhs(du, u, L.p, tstage(t, RP(c3), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd3 * L.dT[i] + (dtC31 * k1[i] + dtC32 * k2[i]);
+  SOLVE(k3);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + RP(a41) * k1[i] + RP(a42) * k2[i] + RP(a43) * k3[i];
+  rhs(du, u, L.p, tstage(t, RP(c4), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd4 * L.dT[i] + (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]);
+  SOLVE(k4);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + RP(a51) * k1[i] + RP(a52) * k2[i] + RP(a53) * k3[i] + RP(a54) * k4[i];
+  rhs(du, u, L.p, tstage(t, RP(c5), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd5 * L.dT[i] + (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]);
+  SOLVE(k5);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + RP(a61) * k1[i] + RP(a62) * k2[i] + RP(a63) * k3[i] + RP(a64) * k4[i] + RP(a65) * k5[i];
+  rhs(du, u, L.p, (float)(t + (Tt)dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC63 * k3[i] + dtC64 * k4[i] + dtC65 * k5[i]);
+  SOLVE(k6);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = u[i] + k6[i];
+  rhs(du, u, L.p, (float)(t + (Tt)dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC71 * k1[i] + dtC72 * k2[i] + dtC73 * k3[i] + dtC74 * k4[i] + dtC75 * k5[i] + dtC76 * k6[i]);
+  SOLVE(k7);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = u[i] + k7[i];
+  rhs(du, u, L.p, (float)(t + (Tt)dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC81 * k1[i] + dtC82 * k2[i] + dtC83 * k3[i] + dtC84 * k4[i] + dtC85 * k5[i] + dtC86 * k6[i] + dtC87 * k7[i]);
+  SOLVE(k8);
+#undef SOLVE
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    uout[i] = u[i] + k8[i];
+    err[i] = k8[i];
+    // dense-output vectors (:139-147, :313-323), consumed only after an accept
+    L.k[0][i] = RP(h21) * k1[i] + RP(h22) * k2[i] + RP(h23) * k3[i] + RP(h24) * k4[i] + RP(h25) * k5[i] + RP(h26) * k6[i] + RP(h27) * k7[i] + RP(h28) * k8[i];
+    L.k[1][i] = RP(h31) * k1[i] + RP(h32) * k2[i] + RP(h33) * k3[i] + RP(h34) * k4[i] + RP(h35) * k5[i] + RP(h36) * k6[i] + RP(h37) * k7[i] + RP(h38) * k8[i];
+    L.k[2][i] = RP(h41) * k1[i] + RP(h42) * k2[i] + RP(h43) * k3[i] + RP(h44) * k4[i] + RP(h45) * k5[i] + RP(h46) * k6[i] + RP(h47) * k7[i] + RP(h48) * k8[i];
+  }
+}
+// stiff/interpolants.jl:13-23
+DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
+  float th1 = 1.0f - th;
+#pragma unroll
+  for (int i = 0; i < N; i++) out[i] = th1 * L.uprev[i] + th * (L.u[i] + th1 * (L.k[0][i] + th * (L.k[1][i] + th * L.k[2][i])));
+}
+#endif
+
+#if DEGPU_ALG <= 3
+// ------------------------------------------------------------------ driver pieces (kernels.jl)
+struct Io {
+  const degpu_kparams& P;
+  DEGPU_DEV Tt* ts(long long i) const { return (Tt*)P.ts + i * P.L; }
+  DEGPU_DEV float* us(long long i) const { return P.us + i * (long long)P.L * N; }
+  DEGPU_DEV Tt saveat(long long i, int l) const {
+    const Tt* s = (const Tt*)P.saveat;
+    return P.saveat_per_traj ? s[i * P.nsaveat + l] : __ldg(s + l);
+  }
+  DEGPU_DEV void store_u(long long i, int l, const float* v) const {
+    float* dst = us(i) + (long long)l * N;
+#pragma unroll
+    for (int c = 0; c < N; c++) dst[c] = v[c];
+  }
+};
+
+// init (nonstiff/types.jl:340-402 et al.) + initial save (kernels.jl:116-126)
+DEGPU_DEV void lane_init(Lane& L, const Io& io, long long i) {
+  const degpu_kparams& P = io.P;
+  const Tt* tsp = (const Tt*)P.tspan + 2 * i;
+  L.t0 = tsp[0];
+  L.tf = tsp[1];
+  L.t = L.t0;
+  L.tprev = L.t0;
+#pragma unroll
+  for (int c = 0; c < N; c++) { L.u[c] = P.u0[i * N + c]; L.uprev[c] = L.u[c]; }
+#pragma unroll
+  for (int c = 0; c < NP; c++) L.p[c] = (c < DEGPU_P) ? P.p[i * DEGPU_P + c] : 0.0f;
+#pragma unroll
+  for (int s = 0; s < NK; s++)
+#pragma unroll
+    for (int c = 0; c < N; c++) L.k[s][c] = L.u[c];
+  float dt = P.dt0 ? P.dt0[i] : (float)(Tt)P.dt;
+  L.dt = dt;
+  L.dtnew = dt;
+  float sc = P.tolscale ? P.tolscale[i] : 1.0f;
+  L.abstol = P.abstol * sc;
+  L.reltol = P.reltol * sc;
+  L.qold = (float)1.0e-4;
+  L.cur_t = 0;
+  L.step_idx = 1;
+  L.nattempt = 0;
+  L.naccept = 0;
+  L.nreject = 0;
+  L.status = DEGPU_RET_DEFAULT;
+  L.need_begin = true;
+  L.fsal = false;
+  if (P.nsaveat) {
+    if (L.t0 == io.saveat(i, 0)) { L.cur_t = 1; io.store_u(i, 0, L.u); }
+  } else {
+    io.store_u(i, 0, L.u);
+  }
+}
+
+// savevalues! (integrator_utils.jl:13-50)
+DEGPU_DEV void save_values(Lane& L, const Io& io, long long i, bool save_everystep) {
+  const degpu_kparams& P = io.P;
+  if (P.nsaveat) {
+    while (L.cur_t < P.nsaveat) {
+      Tt savet = io.saveat(i, L.cur_t);
+      if (!(savet <= L.t)) break;
+      float th = (float)((savet - L.tprev) / (Tt)L.dt);
+      if (L.cur_t < P.L) {
+        float v[N];
+        interp(L, th, L.dt, v);
+        io.store_u(i, L.cur_t, v);
+      }
+      L.cur_t++;
+    }
+  } else if (save_everystep) {
+    if (L.step_idx < P.L) { io.store_u(i, L.step_idx, L.u); io.ts(i)[L.step_idx] = L.t; }
+    L.step_idx++;
+  }
+}
+
+// PI controller, integrator_utils.jl:1-11 constants, decision as in
+// gpu_tsit5_perform_step.jl:124-170.  Returns true on accept.
+DEGPU_DEV bool controller(Lane& L, float EEst, float& dt, Tt t) {
+  const float beta1 = (float)(7.0 / (10.0 * ORDER)), beta2 = (float)(2.0 / (5.0 * ORDER));
+  const float qmax = 10.0f, qmin = (float)(1.0 / 5.0), gamma = (float)(9.0 / 10.0), qoldinit = (float)1.0e-4;
+  float q11 = 0.0f, q;
+  if (EEst == 0.0f) q = 1.0f / qmax;
+  else { q11 = ctrl_pow(EEst, beta1); q = q11 / ctrl_pow(L.qold, beta2); }
+  if (EEst > 1.0f) {
+    dt = dt / jl_min(1.0f / qmin, q11 / gamma);
+    return false;
+  }
+  q = jl_max(1.0f / qmax, jl_min(1.0f / qmin, q / gamma));
+  L.qold = jl_max(EEst, qoldinit);
+  float dtnew = dt / q;
+  Tt rem = L.tf - t - (Tt)dt;
+  L.dtnew = (float)(Tt)jl_mind((double)fabsf(dtnew), fabs((double)rem));
+  L.dt = dt;
+  L.tprev = t;
+  L.t = (rem < (Tt)1.0e-14) ? L.tf : t + (Tt)dt;  // end snap (:155-156)
+  return true;
+}
+
+// One attempt of step!.  Returns true when the trajectory is finished.
+template <bool ADAPTIVE>
+DEGPU_DEV bool advance(Lane& L, const Io& io, long long i) {
+  const degpu_kparams& P = io.P;
+  if (L.need_begin) {
+#pragma unroll
+    for (int c = 0; c < N; c++) L.uprev[c] = L.u[c];
+    begin_step(L);
+    L.need_begin = false;
+  }
+  Tt t = L.t;
+  float unew[N], err[N];
+  if (ADAPTIVE) {
+    float dt = L.dtnew;
+    if (dt < 1.0e-14f) { L.status = DEGPU_RET_DTLESSTHANMIN; return true; }
+    if (++L.nattempt > P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
+    attempt<true>(L, t, dt, unew, err);
+    float EEst = scaled_norm(err, L.uprev, unew, L.abstol, L.reltol);
+    if (!controller(L, EEst, dt, t)) {
+      L.dtnew = dt;
+      L.nreject++;
+      return false;
+    }
+  } else {
+    if (++L.nattempt > P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
+    float dt = L.dt;
+    L.tprev = t;
+    L.t = t + (Tt)dt;
+    attempt<false>(L, t, dt, unew, err);
+  }
+#pragma unroll
+  for (int c = 0; c < N; c++) L.u[c] = unew[c];
+  L.naccept++;
+  L.need_begin = true;
+  save_values(L, io, i, !ADAPTIVE && P.save_everystep);
+  return !(L.t < L.tf);
+}
+
+// end of the driver loop (kernels.jl:53-62, 133-142) and outputs
+DEGPU_DEV void lane_finish(Lane& L, const Io& io, long long i) {
+  const degpu_kparams& P = io.P;
+  Tt* ts = io.ts(i);
+  if (P.nsaveat) {
+    for (int l = 0; l < P.L; l++) ts[l] = (l < L.cur_t) ? io.saveat(i, l) : L.t0;
+  } else {
+    int first_unset = P.save_everystep ? (L.step_idx < P.L ? L.step_idx : P.L) : 1;
+    ts[0] = L.t0;
+    for (int l = first_unset; l < P.L; l++) ts[l] = L.t0;
+    if (L.t > L.tf && P.save_everystep) {
+      float v[N];
+      interp(L, (float)((L.tf - L.tprev) / (Tt)L.dt), L.dt, v);
+      io.store_u(i, P.L - 1, v);
+      ts[P.L - 1] = L.tf;
+    }
+    if (!P.save_everystep) { io.store_u(i, 1, L.u); ts[1] = L.t; }
+  }
+  if (L.status == DEGPU_RET_DEFAULT) {
+    bool fin = true;
+#pragma unroll
+    for (int c = 0; c < N; c++) fin = fin && isfinite(L.u[c]);
+    L.status = fin ? DEGPU_RET_SUCCESS : DEGPU_RET_UNSTABLE;
+  }
+  if (P.retcode) P.retcode[i] = (signed char)L.status;
+  if (P.naccept) P.naccept[i] = L.naccept;
+  if (P.nreject) P.nreject[i] = L.nreject;
+}
+#endif  // DEGPU_ALG <= 3
+
+}  // namespace degpu
+
+// ------------------------------------------------------------------ entry points
+#if DEGPU_DRIVER == 0 || DEGPU_DRIVER == 1
+// ode_solve_kernel / ode_asolve_kernel (kernels.jl:1-152): one trajectory per thread.
+extern "C" __global__ void __launch_bounds__(256) degpu_solve_kernel(const degpu_kparams P) {
+  using namespace degpu;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.B) return;
+  Io io{P};
+  Lane L;
+  lane_init(L, io, i);
+  bool done = !(L.t < L.tf);
+  while (!done) done = advance<DEGPU_DRIVER == 1>(L, io, i);
+  lane_finish(L, io, i);
+}
+#endif
+
+#if DEGPU_DRIVER == 2
+// Persistent adaptive driver.  Each warp claims `chunk` trajectories at a time from a
+// global counter (work stealing between warps); inside the warp a lane that finishes
+// its trajectory immediately takes the next one (lane refill), so every lane keeps
+// stepping while trajectories of very different lengths (uneven step counts, per-
+// trajectory tspans) drain.  Every trajectory is bounded by maxiters attempts, so the
+// loop ends: each pass either advances some lane or hands out work, and no lane ever
+// waits on another warp or block.
+extern "C" __global__ void __launch_bounds__(256) degpu_persistent_kernel(const degpu_kparams P) {
+  using namespace degpu;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  Io io{P};
+  Lane L;
+  long long my = -1;
+  long long q_next = 0, q_end = 0;
+  bool exhausted = false;
+  const long long B = P.B;
+  const int chunk = P.chunk > 0 ? P.chunk : 32;
+  for (;;) {
+    unsigned idle = __ballot_sync(FULL, my < 0);
+    if (idle) {
+      if (q_next >= q_end && !exhausted) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(P.work, (unsigned long long)chunk);
+        base = __shfl_sync(FULL, base, 0);
+        if ((long long)base >= B) exhausted = true;
+        else { q_next = (long long)base; q_end = min((long long)base + chunk, B); }
+      }
+      int rank = __popc(idle & lt_mask);
+      if (my < 0 && q_next + rank < q_end) {
+        my = q_next + rank;
+        lane_init(L, io, my);
+        if (!(L.t < L.tf)) { lane_finish(L, io, my); my = -1; }
+      }
+      q_next = min(q_next + (long long)__popc(idle), q_end);
+    }
+    if (__ballot_sync(FULL, my >= 0) == 0) {
+      if (exhausted) break;
+      continue;
+    }
+    if (my >= 0) {
+      if (advance<true>(L, io, my)) { lane_finish(L, io, my); my = -1; }
+    }
+  }
+}
+#endif
+
+#if DEGPU_DRIVER == 3
+// em_kernel (perform_step/gpu_em_perform_step.jl:1-74).  The reference seeds Julia's
+// device RNG with prob.seed; here each trajectory draws from a counter-based
+// Philox4x32-10 stream (Salmon et al., SC'11) keyed by `seed`, counter
+// (step, trajectory, block), with Box-Muller normals.
+namespace degpu {
+DEGPU_DEV void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+    uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+}
+DEGPU_DEV void normals4(uint64_t seed, uint32_t step, uint32_t traj, uint32_t blk, float* z) {
+  uint32_t c[4] = {step, traj, blk, 0u};
+  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    float u1 = (float)((c[2 * h] >> 8) + 1u) * 5.9604645e-08f;
+    float u2 = (float)(c[2 * h + 1] >> 8) * 5.9604645e-08f;
+#if DEGPU_PARITY
+    float r = sqrtf(-2.0f * pm_logf(u1));
+    float s, co;
+    pm_sincos_turns(u2, &s, &co);
+#else
+    float r = sqrtf(-2.0f * __logf(u1));
+    float s, co;
+    __sincosf(6.28318531f * u2, &s, &co);
+#endif
+    z[2 * h] = r * co;
+    z[2 * h + 1] = r * s;
+  }
+}
+}  // namespace degpu
+
+extern "C" __global__ void __launch_bounds__(256) degpu_em_kernel(const degpu_kparams P) {
+  using namespace degpu;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.B) return;
+  const int L = P.L;
+  const Tt* tsp = (const Tt*)P.tspan + 2 * i;
+  Tt t0 = tsp[0], tf = tsp[1];
+  Tt dtT = (Tt)P.dt;
+  float dt = (float)dtT;
+  Tt* ts = (Tt*)P.ts + i * L;
+  float* us = P.us + i * (long long)L * N;
+  const Tt* sa = P.nsaveat ? (const Tt*)P.saveat + (P.saveat_per_traj ? i * P.nsaveat : 0) : nullptr;
+  int cur_t = 0;
+  float p[NP];
+#pragma unroll
+  for (int c = 0; c < NP; c++) p[c] = (c < DEGPU_P) ? P.p[i * DEGPU_P + c] : 0.0f;
+  float u[N], up[N], f[N], g[N], z[(N + 3) / 4 * 4];
+#pragma unroll
+  for (int c = 0; c < N; c++) u[c] = P.u0[i * N + c];
+  for (int l = 0; l < L; l++) ts[l] = t0;
+  if (sa) {
+    if (t0 == sa[0]) { cur_t = 1; for (int c = 0; c < N; c++) us[c] = u[c]; }
+  } else {
+    for (int c = 0; c < N; c++) us[c] = u[c];
+  }
+  float sqdt = sqrtf(dt);
+  Tt t = t0;
+  Tt span = tf - t0;
+  Tt ratio = (span < 0 ? -span : span) / (dtT < 0 ? -dtT : dtT);
+  long long n = (long long)floor((double)ratio) + 1;
+  if (n - 1 > P.maxiters) n = P.maxiters + 1;
+  const uint32_t gi = (uint32_t)(P.traj_offset + i);
+  for (long long j = 2; j <= n; j++) {
+#pragma unroll
+    for (int c = 0; c < N; c++) up[c] = u[c];
+    degpu_f<float>(f, up, p, (float)t);
+    degpu_g<float>(g, up, p, (float)t);
+#pragma unroll
+    for (int b = 0; b < (N + 3) / 4; b++) normals4(P.seed, (uint32_t)(j - 2), gi, (uint32_t)b, z + 4 * b);
+#pragma unroll
+    for (int c = 0; c < N; c++) u[c] = up[c] + f[c] * dt + (sqdt * g[c]) * z[c];
+    t = t + (Tt)dt;
+    if (!sa && P.save_everystep) {
+      if (j - 1 < L) { for (int c = 0; c < N; c++) us[(j - 1) * N + c] = u[c]; ts[j - 1] = t; }
+    } else if (sa) {
+      while (cur_t < P.nsaveat && sa[cur_t] <= t) {
+        Tt savet = sa[cur_t];
+        float th = (float)((savet - (t - (Tt)dt)) / (Tt)dt);
+        if (cur_t < L) { for (int c = 0; c < N; c++) us[cur_t * N + c] = up[c] + (u[c] - up[c]) * th; ts[cur_t] = savet; }
+        cur_t++;
+      }
+    }
+  }
+  if (!sa && !P.save_everystep) { for (int c = 0; c < N; c++) us[N + c] = u[c]; ts[1] = t; }
+  if (P.retcode) {
+    bool fin = true;
+    for (int c = 0; c < N; c++) fin = fin && isfinite(u[c]);
+    P.retcode[i] = fin ? DEGPU_RET_SUCCESS : DEGPU_RET_UNSTABLE;
+  }
+}
+#endif

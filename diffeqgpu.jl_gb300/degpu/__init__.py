@@ -1,0 +1,15 @@
+"""degpu -- GB300-native EnsembleGPUKernel engine (DiffEqGPU.jl's kernel path).
+
+The solver kernels are hand-written CUDA for sm_103a, JIT-compiled together with the
+user's CUDA C right-hand side by libdegpu.so (C ABI: include/degpu.h).  This package is
+the Python mirror of the reference's interface; there is no CPU fallback.
+"""
+from ._lib import DegpuError, RETCODE_NAMES, lib  # noqa: F401
+from .api import (  # noqa: F401
+    DeviceProblems, EnsembleGPUKernel, EnsembleProblem, EnsembleSolution, GPUEM, GPURodas5, GPURodas5P,
+    GPURosenbrock23, GPUTsit5, GPUVern7, LinRange, ODEFunction, ODEProblem, ODESolution, Range, SDEFunction,
+    SDEProblem, adapt, alg_order, make_prob_compatible, normalize_saveat, remake, solve, vectorized_asolve,
+    vectorized_solve,
+)
+
+__version__ = "0.1.0"

@@ -1,0 +1,75 @@
+"""Algorithmic FP32 operation counts per step attempt, for roofline accounting.
+
+Convention: each IEEE add, sub, mul, div = 1 flop (an FMA = 2), sqrt and pow counted as
+1 each; only operations the method needs are counted (the reference's redundant Vern7
+k1 recomputation and the Rosenbrock re-solves of W are not).  A stage combination
+uprev + dt*(sum of m terms a_j k_j) costs 2m+1 flops per component; the embedded error
+dt*(sum of m terms) costs 2m.  RHS costs are per evaluation.
+"""
+from __future__ import annotations
+
+RHS_FLOPS = {"lorenz": 8, "robertson": 13, "decay": 2, "growth": 0, "osc": 3, "linear15": 15}
+
+# number of terms in each stage combination (excluding uprev), the solution update and
+# the error estimate; number of RHS evaluations per attempt (first-same-as-last for Tsit5)
+_TSIT5 = dict(stages=[1, 2, 3, 4, 5], update=6, err=7, rhs=6, stage_times=5)
+_VERN7 = dict(stages=[1, 2, 2, 3, 4, 5, 6, 7, 6], update=7, err=8, rhs=10, stage_times=9)
+
+
+def _explicit(spec, N, rhs, adaptive):
+    f = sum(2 * m + 1 for m in spec["stages"]) * N
+    f += (2 * spec["update"] + 1) * N
+    f += spec["rhs"] * rhs
+    f += 2 * spec["stage_times"]
+    if adaptive:
+        f += 2 * spec["err"] * N          # error combination
+        f += 5 * N + 2                    # weights, squares, norm
+        f += 12                           # controller (2 pow, clamps, divisions, time update)
+    return f
+
+
+def attempt_flops(alg: str, N: int, model: str, adaptive: bool = True) -> int:
+    rhs = RHS_FLOPS[model]
+    if alg == "tsit5":
+        return _explicit(_TSIT5, N, rhs, adaptive)
+    if alg == "vern7":
+        return _explicit(_VERN7, N, rhs, adaptive) - rhs  # k1 once per step, counted in step_flops
+    if alg == "rosenbrock23":
+        lu = 2 * N ** 3 // 3 + N * N          # factor W
+        solve = 2 * N * N                      # one triangular pair
+        return 2 * N * N + lu + 3 * solve + 3 * rhs + 14 * N + (5 * N + 14 if adaptive else 0)
+    if alg == "rodas5p":
+        lu = 2 * N ** 3 // 3 + N * N
+        solve = 2 * N * N
+        return 28 + 6 + N * N + lu + 8 * solve + 8 * rhs + 120 * N + (5 * N + 14 if adaptive else 0)
+    raise ValueError(alg)
+
+
+def step_flops(alg: str, N: int, model: str) -> int:
+    """Per accepted step, work done once per step (not per attempt)."""
+    rhs = RHS_FLOPS[model]
+    if alg == "vern7":
+        return rhs
+    if alg in ("rosenbrock23", "rodas5p"):
+        return 3 * rhs * N  # Jacobian by forward-mode AD ~ N dual sweeps
+    return 0
+
+
+def interp_flops(alg: str, N: int, model: str) -> int:
+    rhs = RHS_FLOPS[model]
+    if alg == "tsit5":
+        return 4 * 7 + (2 * 7 + 1) * N + 2
+    if alg == "vern7":
+        return 13 * 12 + 6 * rhs + (2 * 9 + 1) * 6 * N + 30 * N
+    if alg == "rosenbrock23":
+        return 8 + 5 * N
+    return 8 + 9 * N
+
+
+def solve_flops(alg: str, N: int, model: str, naccept, nreject, nsaves) -> float:
+    """Total algorithmic flops of a solve from the per-trajectory counters."""
+    import numpy as np
+    na = np.asarray(naccept, dtype=np.float64).sum()
+    nr = np.asarray(nreject, dtype=np.float64).sum()
+    return ((na + nr) * attempt_flops(alg, N, model, True) + na * step_flops(alg, N, model)
+            + float(nsaves) * interp_flops(alg, N, model))

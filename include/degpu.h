@@ -1,0 +1,187 @@
+/* degpu -- C ABI of the GB300 EnsembleGPUKernel engine (libdegpu.so).
+ *
+ * Drop-in boundary for DiffEqGPU.jl's lower-level kernel API: a Julia shim (ccall) or any
+ * C caller passes caller-owned DEVICE buffers and a CUDA stream; every solve is
+ * stream-ordered (no host synchronisation inside), returns 0 or a negative DEGPU_E*
+ * code, and reports per-trajectory failures in retcode[] instead of trapping.
+ * Plain C types only; the stream is a cudaStream_t passed as void*.
+ *
+ * Layouts (B trajectories, N states, P parameters, L saved rows, Tt = time type):
+ *   u0 [B][N] f32, p [B][P] f32, tspan [B][2] Tt, saveat [L] or [B][L] Tt,
+ *   ts [B][L] Tt, us [B][L][N] f32  -- ts/us are the column-major Julia matrices
+ *   Matrix{Tt}(L, B) and Matrix{SVector{N,Float32}}(L, B) of the reference.
+ */
+#ifndef DEGPU_H
+#define DEGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DEGPU_VERSION "0.1.0"
+
+/* return codes */
+#define DEGPU_OK 0
+#define DEGPU_E_INVALID (-1)   /* bad argument (sizes, pointers, options) */
+#define DEGPU_E_COMPILE (-2)   /* NVRTC failed on the right-hand side or kernels */
+#define DEGPU_E_CUDA (-3)      /* CUDA driver/runtime error */
+#define DEGPU_E_UNSUPPORTED (-4) /* combination the reference also rejects */
+
+/* algorithms: GPUTsit5, GPUVern7, GPURosenbrock23, GPURodas5P (alias GPURodas5), GPUEM
+ * (src/ensemblegpukernel/gpukernel_algorithms.jl:30, 57, 112, 162, 243) */
+#define DEGPU_ALG_TSIT5 0
+#define DEGPU_ALG_VERN7 1
+#define DEGPU_ALG_ROSENBROCK23 2
+#define DEGPU_ALG_RODAS5P 3
+#define DEGPU_ALG_EM 4
+
+#define DEGPU_TIME_F32 0 /* Float32 tspan: every operation is the reference's Float32 one */
+#define DEGPU_TIME_F64 1 /* FP64 time accumulation / end detection, FP32 state */
+
+#define DEGPU_MODE_FAST 0   /* FMA contraction, hardware pow, LU + refinement */
+#define DEGPU_MODE_PARITY 1 /* strict IEEE order of the reference, portable pow, Cramer solves */
+
+#define DEGPU_DRIVER_AUTO 0       /* fixed: one trajectory/thread; adaptive: persistent */
+#define DEGPU_DRIVER_NAIVE 1      /* one trajectory per thread (ode_asolve_kernel shape) */
+#define DEGPU_DRIVER_PERSISTENT 2 /* warp lane refill + work stealing */
+
+#define DEGPU_JAC_AUTO 0       /* user Jacobian/tgrad if given, else forward-mode AD */
+#define DEGPU_JAC_AD 1
+#define DEGPU_JAC_FINITEDIFF 2 /* alg_utils.jl:17-27 */
+
+/* per-trajectory retcodes */
+#define DEGPU_RET_DEFAULT 0
+#define DEGPU_RET_SUCCESS 1
+#define DEGPU_RET_TERMINATED 2
+#define DEGPU_RET_DTLESSTHANMIN 3
+#define DEGPU_RET_MAXITERS 4
+#define DEGPU_RET_UNSTABLE 5
+
+/* right-hand side flags */
+#define DEGPU_RHS_HAS_JAC 1   /* source defines degpu_jac(float* J, const float* u, const float* p, float t), J column-major */
+#define DEGPU_RHS_HAS_TGRAD 2 /* source defines degpu_tgrad(float* dT, const float* u, const float* p, float t) */
+#define DEGPU_RHS_HAS_NOISE 4 /* source defines template<class T> degpu_g(T* g, const T* u, const float* p, T t) (diagonal noise) */
+
+typedef struct degpu_rhs_s degpu_rhs;
+typedef struct degpu_plan_s degpu_plan;
+
+/* The isbits ImmutableODEProblem array of the reference, flattened (device pointers). */
+typedef struct degpu_problems {
+  const float* u0;    /* [B][N] */
+  const float* p;     /* [B][P] */
+  const void* tspan;  /* [B][2] of the time type */
+  long long B;
+} degpu_problems;
+
+/* keyword arguments of vectorized_solve / vectorized_asolve */
+typedef struct degpu_options {
+  int alg;              /* DEGPU_ALG_* */
+  int time_type;        /* DEGPU_TIME_* */
+  int mode;             /* DEGPU_MODE_* */
+  int driver;           /* DEGPU_DRIVER_* */
+  int jac;              /* DEGPU_JAC_* */
+  int save_everystep;
+  int nsaveat;          /* 0 = no saveat */
+  int saveat_per_traj;
+  const void* saveat;   /* device, time type */
+  double dt;            /* fixed dt, or initial dt of the adaptive controller */
+  double abstol;
+  double reltol;
+  long long maxiters;   /* cap on step attempts per trajectory (0 = 10^7) */
+  const float* dt0;     /* optional device [B]: per-trajectory initial dt (learned controller) */
+  const float* tolscale;/* optional device [B]: per-trajectory tolerance multiplier */
+  unsigned long long seed; /* EM noise key */
+  long long traj_offset;   /* global index of trajectory 0 (noise streams of shards) */
+  int block;            /* threads per block (0 = autotuned/default) */
+  int chunk;            /* persistent driver: trajectories per warp refill (0 = default) */
+} degpu_options;
+
+/* outputs (caller-owned device buffers) */
+typedef struct degpu_outputs {
+  void* ts;             /* [B][L] time type */
+  float* us;            /* [B][L][N] */
+  int L;
+  signed char* retcode; /* optional [B] */
+  int* naccept;         /* optional [B] */
+  int* nreject;         /* optional [B] */
+} degpu_outputs;
+
+const char* degpu_version(void);
+/* last error message of the calling thread */
+const char* degpu_last_error(void);
+
+/* Register a right-hand side written in CUDA C:
+ *   template <class T> __device__ void degpu_f(T* du, const T* u, const float* p, T t);
+ * (T is float or a forward-mode dual), plus the optional functions named by flags.  It is
+ * compiled with NVRTC for sm_103a together with the steppers, so it is inlined into
+ * them.  Replaces the Julia RHS that the reference compiles into its KernelAbstractions
+ * kernel (src/ensemblegpukernel/kernels.jl:1-152 via prob.f). */
+int degpu_rhs_create(const char* cuda_source, int n_state, int n_param, int flags, degpu_rhs** out);
+void degpu_rhs_destroy(degpu_rhs* f);
+/* Source of a built-in model ("lorenz", "robertson", "decay", "growth", "linear15",
+ * "gbm", "lorenz_addnoise", "osc"); NULL if unknown.  Also returns N, P, flags. */
+const char* degpu_builtin_rhs(const char* name, int* n_state, int* n_param, int* flags);
+
+/* vectorized_solve(probs, prob::ODEProblem, alg; dt, saveat, save_everystep)
+ * -- src/ensemblegpukernel/lowerlevel_solve.jl:53-131 (fixed step). */
+int degpu_vectorized_solve(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
+                           degpu_outputs* out, void* stream);
+
+/* vectorized_asolve(probs, prob::ODEProblem, alg; dt, saveat, abstol, reltol)
+ * -- src/ensemblegpukernel/lowerlevel_solve.jl:253-346 (adaptive). */
+int degpu_vectorized_asolve(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
+                            degpu_outputs* out, void* stream);
+
+/* vectorized_solve(probs, prob::SDEProblem, GPUEM(); dt, saveat, save_everystep)
+ * -- src/ensemblegpukernel/lowerlevel_solve.jl:134-199 with em_kernel
+ * (perform_step/gpu_em_perform_step.jl:1-74).  Adaptive EM is rejected like
+ * lowerlevel_solve.jl:348-356. */
+int degpu_vectorized_solve_sde(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
+                               degpu_outputs* out, void* stream);
+
+/* batch_solve_up_kernel (src/solve.jl:382-419) with HOST buffers: copies the problems
+ * to the device, runs vectorized_(a)solve, copies ts/us (and retcodes) back and
+ * synchronises.  adaptive selects vectorized_asolve.  Host arrays use the layouts above. */
+int degpu_batch_solve_host(const degpu_rhs* f, const float* u0, const float* p, const void* tspan, long long B,
+                           const degpu_options* opt, int adaptive, void* ts, float* us, int L,
+                           signed char* retcode, int* naccept, int* nreject, void* stream);
+
+/* Solve plan: compiles, autotunes block size and trajectories-per-warp (when
+ * opt->block == 0), allocates the work counter and captures the whole solve (counter
+ * reset + kernel) in a CUDA graph, so that repeated solves over the same buffers are one
+ * graph launch.  adaptive selects vectorized_asolve semantics. */
+int degpu_plan_create(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt, int adaptive,
+                      degpu_outputs* out, void* stream, degpu_plan** plan);
+int degpu_plan_launch(degpu_plan* plan, void* stream);
+/* the configuration the plan chose: block, chunk, grid, driver, registers per thread */
+int degpu_plan_info(const degpu_plan* plan, int* block, int* chunk, int* grid, int* driver, int* regs);
+void degpu_plan_destroy(degpu_plan* plan);
+
+/* Autotuner (block size, trajectories per warp refill) on the first sample_B
+ * trajectories; results are cached per kernel and size class. */
+int degpu_autotune(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt, int adaptive,
+                   degpu_outputs* out, long long sample_B, void* stream, int* best_block, int* best_chunk);
+
+/* Compile (NVRTC, sm_103a) the kernel a solve with these options would use, without
+ * loading it -- needs no GPU.  Reports the compiler log on failure through
+ * degpu_last_error().  *cubin_bytes receives the size of the compiled image. */
+int degpu_rhs_check(const degpu_rhs* f, const degpu_options* opt, int adaptive, long long* cubin_bytes);
+
+/* Registers/thread and spill bytes of the kernel a solve with these options would use
+ * (compiles it if needed). */
+int degpu_kernel_info(const degpu_rhs* f, const degpu_options* opt, int adaptive, int* regs, int* local_bytes,
+                      int* max_threads);
+
+/* ---- measurement utilities (no counterpart in the reference) ---- */
+/* Sustained FP32 FMA throughput of the current device in TFLOP/s (8 independent FMA
+ * chains per thread over a grid that fills every SM); the roofline denominator that
+ * bench.py reports the stepping kernels against. */
+int degpu_fp32_peak(double* tflops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,124 @@
+#!/usr/bin/env python3
+"""Generate the Butcher/Rosenbrock tableau headers from DiffEqGPU.jl's tableau files.
+
+Test-infrastructure / build-time recipe.  It reads the reference's tableau sources
+(read-only) and writes two headers with the SAME numbers:
+
+  * ``oracle/tableaus_gen.h``                         -- FP64 literals for the CPU oracle
+  * ``diffeqgpu.jl_gb300/csrc/device/tableaus_gen.cuh`` -- FP32 ``__constant__`` arrays for
+    the kernels.
+
+The reference writes every coefficient as ``name = convert(T, <Float64 literal>)``
+(``src/ensemblegpukernel/tableaus/verner_tableaus.jl`` and ``rodas_tableaus.jl``) and
+Julia's ``convert(Float32, x::Float64)`` rounds to nearest.  The device header stores
+``float(np.float32(np.float64(literal)))`` printed with enough digits to round-trip,
+so the kernels see bit-identical coefficients.
+
+Run once in a checkout that has the reference mounted:
+    python oracle/gen_tableaus.py /root/reference
+The outputs are committed; nothing at run time reads the reference.
+"""
+import re
+import sys
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent.parent
+
+# (table name, file, julia function, first line, last line) -- line ranges are cited in the headers
+TABLES = [
+    ("vern7", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern7Tableau"),
+    ("vern7x", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern7ExtraStages"),
+    ("vern7i", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern7InterpolationCoefficients"),
+    ("vern9", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern9Tableau"),
+    ("rodas5p", "src/ensemblegpukernel/tableaus/rodas_tableaus.jl", "Rodas5PTableau"),
+]
+
+ASSIGN = re.compile(r"^\s*([A-Za-z_γ][A-Za-z0-9_γ]*)\s*=\s*convert\(\s*T2?\s*,\s*([-+0-9.eE]+)\s*\)\s*$")
+
+
+def parse_function(path: Path, fname: str):
+    lines = path.read_text().splitlines()
+    start = None
+    for i, ln in enumerate(lines):
+        if re.match(rf"^function {fname}\(", ln):
+            start = i
+            break
+    if start is None:
+        raise SystemExit(f"{fname} not found in {path}")
+    out = []
+    end = start
+    for j in range(start + 1, len(lines)):
+        ln = lines[j]
+        if ln.startswith("end"):
+            end = j
+            break
+        m = ASSIGN.match(ln)
+        if m:
+            name = m.group(1).replace("γ", "gamma")
+            out.append((name, float(m.group(2))))
+    return out, start + 1, end + 1
+
+
+def f32_literal(x: float) -> str:
+    v = float(np.float32(np.float64(x)))
+    s = repr(v)
+    if "e" not in s and "." not in s:
+        s += ".0"
+    return s + "f"
+
+
+def main():
+    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    oracle_lines = [
+        "/* Generated by oracle/gen_tableaus.py -- do not edit.",
+        " * FP64 coefficient literals of DiffEqGPU.jl's tableaus (see per-table citations).",
+        " * Oracle (test infrastructure) copy; the kernels get the same numbers in tableaus_gen.cuh. */",
+        "#pragma once",
+        "",
+    ]
+    dev_lines = [
+        "// Generated by oracle/gen_tableaus.py -- do not edit.",
+        "// Method coefficients (Verner 7(6), Rodas5P) rounded once from their published FP64",
+        "// values to FP32, exactly as Julia's convert(Float32, ::Float64) does in the reference",
+        "// (see per-table citations).  They live in constant memory and are read as",
+        "// constant-bank operands by the stage arithmetic.",
+        "#pragma once",
+        "",
+    ]
+    for tab, rel, fname in TABLES:
+        entries, l0, l1 = parse_function(ref / rel, fname)
+        cite = f"{rel}:{l0}-{l1} ({fname})"
+        names = [n for n, _ in entries]
+        oracle_lines.append(f"/* {cite} */")
+        oracle_lines.append("enum {")
+        for n in names:
+            oracle_lines.append(f"  OR_{tab.upper()}_{n},")
+        oracle_lines.append(f"  OR_{tab.upper()}_COUNT")
+        oracle_lines.append("};")
+        oracle_lines.append(f"static const double OR_{tab.upper()}[OR_{tab.upper()}_COUNT] = {{")
+        for n, v in entries:
+            oracle_lines.append(f"  {v!r}, /* {n} */")
+        oracle_lines.append("};")
+        oracle_lines.append("")
+        if tab == "vern9":
+            continue  # FP64 oracle method only
+        dev_lines.append(f"// {cite}")
+        dev_lines.append("enum {")
+        for n in names:
+            dev_lines.append(f"  {tab.upper()}_{n},")
+        dev_lines.append(f"  {tab.upper()}_COUNT")
+        dev_lines.append("};")
+        dev_lines.append(f"__constant__ float c_{tab}[{tab.upper()}_COUNT] = {{")
+        for n, v in entries:
+            dev_lines.append(f"  {f32_literal(v)}, // {n}")
+        dev_lines.append("};")
+        dev_lines.append("")
+    (REPO / "oracle" / "tableaus_gen.h").write_text("\n".join(oracle_lines) + "\n")
+    (REPO / "diffeqgpu.jl_gb300" / "csrc" / "device" / "tableaus_gen.cuh").write_text("\n".join(dev_lines) + "\n")
+    print("wrote oracle/tableaus_gen.h and diffeqgpu.jl_gb300/csrc/device/tableaus_gen.cuh")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1125 @@
+/* CPU oracle for the EnsembleGPUKernel hot path of DiffEqGPU.jl -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py (CPU-baseline leg and the
+ * `--impl reference` arm) load this library, and only as the checker / the timed CPU
+ * reference.  The product (libdegpu.so + its kernels) never links or calls it.
+ *
+ * What it restates (all paths relative to the DiffEqGPU.jl checkout):
+ *   driver loops        src/ensemblegpukernel/kernels.jl:1-152 (ode_solve_kernel, ode_asolve_kernel)
+ *   saveat / sizing     src/ensemblegpukernel/lowerlevel_solve.jl:53-131, 253-346
+ *   savevalues!         src/ensemblegpukernel/integrators/integrator_utils.jl:13-50
+ *   controller consts   src/ensemblegpukernel/integrators/integrator_utils.jl:1-11
+ *   Tsit5 step!         src/ensemblegpukernel/perform_step/gpu_tsit5_perform_step.jl:1-175
+ *   Vern7 step!         src/ensemblegpukernel/perform_step/gpu_vern7_perform_step.jl:1-210
+ *   Rosenbrock23 step!  src/ensemblegpukernel/perform_step/gpu_rosenbrock23_perform_step.jl:1-201
+ *   Rodas5P step!       src/ensemblegpukernel/perform_step/gpu_rodas5P_perform_step.jl:1-351
+ *   EM kernel           src/ensemblegpukernel/perform_step/gpu_em_perform_step.jl:1-74
+ *   interpolants        src/ensemblegpukernel/integrators/nonstiff/interpolants.jl:28-190, 372-399,
+ *                       src/ensemblegpukernel/integrators/stiff/interpolants.jl:13-23
+ *   3x3 linear solve    src/ensemblegpukernel/linalg/linsolve.jl:31-57 (Cramer's rule)
+ *   J / tgrad           src/ensemblegpukernel/nlsolve/type.jl:129-157, alg_utils.jl:17-27
+ *   norm                DiffEqBase.ODE_DEFAULT_NORM for static arrays: sqrt(sum(abs2,u)/length(u))
+ *
+ * Arithmetic is FP32 in the reference's operation order (n-ary `+` folds left,
+ * `dt*a*k` = `(dt*a)*k`), built with -ffp-contract=off.  Coefficients come from
+ * tableaus_gen.h (Vern7, Rodas5P, Vern9; generated from the reference's tableau files)
+ * and, for Tsit5, from Tsitouras (2011) -- the reference takes them from the un-vendored
+ * SimpleDiffEq 1.11 (`_build_tsit5_caches`, `bθs`); their order conditions are checked
+ * in tests/test_oracle.py.
+ *
+ * Documented deviations from the reference (the same in the kernels' parity mode):
+ *   - `EEst^beta1`, `qold^beta2` use pm_powf (portable_math.h), not libm/CUDA pow;
+ *   - interpolants (`@muladd` in the reference) are evaluated without FMA;
+ *   - `error("dt<dtmin")` becomes retcode DtLessThanMin, and an attempt cap (maxiters)
+ *     ends runaway trajectories with retcode MaxIters instead of looping forever;
+ *   - time may be FP64 (Tt = double) with FP32 state.  With Tt = float every operation
+ *     is the reference's Float32 operation.
+ * Parity status: bit-faithful restatement for the fixed-step explicit RK path (only
+ * +,-,* in a fixed order); adaptive paths pinned by the FP64 Vern9 solution and the
+ * reference's own test tolerances -- the reference (Julia) cannot run in this build.
+ *
+ * Also here: an FP64 Vern9 solver (tableau: tableaus/verner_tableaus.jl:1198-1332) used
+ * as the high-accuracy error oracle, and OpenMP ensemble drivers (the timed CPU baseline).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+
+#include "portable_math.h"
+#include "tableaus_gen.h"
+
+/* ------------------------------------------------------------------ constants */
+enum { ALG_TSIT5 = 0, ALG_VERN7 = 1, ALG_RB23 = 2, ALG_RODAS5P = 3, ALG_EM = 4 };
+enum { RET_DEFAULT = 0, RET_SUCCESS = 1, RET_TERMINATED = 2, RET_DTMIN = 3, RET_MAXITERS = 4, RET_UNSTABLE = 5 };
+enum { JAC_AD = 0, JAC_ANALYTIC = 1, JAC_FINITEDIFF = 2 };
+enum {
+  M_LORENZ = 0, M_ROBERTSON = 1, M_DECAY = 2, M_GROWTH = 3, M_LINEAR15 = 4,
+  M_GBM = 5, M_LORENZ_ADDNOISE = 6, M_OSC = 7
+};
+#define MAXN 16
+#define MAXP 8
+
+/* ------------------------------------------------------------------ dual numbers
+ * Forward-mode duals with NP partials, product rule ordered like ForwardDiff's
+ * `x*y -> (vx*vy, partials(x)*vy + partials(y)*vx)`. */
+template <int NP> struct Dual {
+  float v; float d[NP];
+  Dual() : v(0.f) { for (int i = 0; i < NP; i++) d[i] = 0.f; }
+  Dual(float x) : v(x) { for (int i = 0; i < NP; i++) d[i] = 0.f; }
+};
+template <int NP> static inline Dual<NP> operator+(Dual<NP> a, Dual<NP> b) { Dual<NP> r; r.v = a.v + b.v; for (int i = 0; i < NP; i++) r.d[i] = a.d[i] + b.d[i]; return r; }
+template <int NP> static inline Dual<NP> operator-(Dual<NP> a, Dual<NP> b) { Dual<NP> r; r.v = a.v - b.v; for (int i = 0; i < NP; i++) r.d[i] = a.d[i] - b.d[i]; return r; }
+template <int NP> static inline Dual<NP> operator-(Dual<NP> a) { Dual<NP> r; r.v = -a.v; for (int i = 0; i < NP; i++) r.d[i] = -a.d[i]; return r; }
+template <int NP> static inline Dual<NP> operator*(Dual<NP> a, Dual<NP> b) { Dual<NP> r; r.v = a.v * b.v; for (int i = 0; i < NP; i++) r.d[i] = a.d[i] * b.v + b.d[i] * a.v; return r; }
+template <int NP> static inline Dual<NP> operator*(float a, Dual<NP> b) { Dual<NP> r; r.v = a * b.v; for (int i = 0; i < NP; i++) r.d[i] = a * b.d[i]; return r; }
+template <int NP> static inline Dual<NP> operator*(Dual<NP> b, float a) { Dual<NP> r; r.v = b.v * a; for (int i = 0; i < NP; i++) r.d[i] = b.d[i] * a; return r; }
+template <int NP> static inline Dual<NP> operator+(float a, Dual<NP> b) { Dual<NP> r = b; r.v = a + b.v; return r; }
+template <int NP> static inline Dual<NP> operator+(Dual<NP> b, float a) { Dual<NP> r = b; r.v = b.v + a; return r; }
+template <int NP> static inline Dual<NP> operator-(float a, Dual<NP> b) { Dual<NP> r; r.v = a - b.v; for (int i = 0; i < NP; i++) r.d[i] = -b.d[i]; return r; }
+template <int NP> static inline Dual<NP> operator-(Dual<NP> b, float a) { Dual<NP> r = b; r.v = b.v - a; return r; }
+
+/* ------------------------------------------------------------------ models
+ * Right-hand sides written with the same operation order as the CUDA C sources the
+ * tests hand to the library (diffeqgpu.jl_gb300/degpu/models.py).  S is float or Dual.
+ *   lorenz     test/gpu_kernel_de/gpu_ode_regression.jl:4-12
+ *   robertson  test/gpu_kernel_de/stiff_ode/gpu_ode_mass_matrix.jl (ODE form of its kinetics)
+ *   decay      test/gpu_kernel_de/stiff_ode/gpu_ode_regression.jl:5-8   (u' = -p1 u)
+ *   growth     test/public_interface.jl:9-11                           (u' = u)
+ *   linear15   test/gpu_kernel_de/stiff_ode/gpu_ode_regression.jl:24-26 (u' = 1.01 u, N=15)
+ *   gbm        test/gpu_kernel_de/gpu_sde_convergence.jl:6-8           (f = p1 u, g = p2 u)
+ *   lorenz+additive noise  test/gpu_kernel_de/gpu_sde_regression.jl:47-58
+ *   osc        harmonic oscillator u1' = u2, u2' = -p1^2 u1 (non-chaotic known answer) */
+struct ModelInfo { int N, P, has_jac, has_tgrad, is_sde; };
+static ModelInfo model_info(int m) {
+  switch (m) {
+    case M_LORENZ: return {3, 3, 1, 1, 0};
+    case M_ROBERTSON: return {3, 3, 1, 1, 0};
+    case M_DECAY: return {1, 1, 1, 1, 0};
+    case M_GROWTH: return {1, 1, 0, 0, 0};
+    case M_LINEAR15: return {15, 1, 0, 0, 0};
+    case M_GBM: return {1, 2, 0, 0, 1};
+    case M_LORENZ_ADDNOISE: return {3, 3, 0, 0, 1};
+    case M_OSC: return {2, 1, 1, 1, 0};
+  }
+  return {0, 0, 0, 0, 0};
+}
+
+template <class S>
+static void model_f(int m, S* du, const S* u, const float* p, float t) {
+  (void)t;
+  switch (m) {
+    case M_LORENZ:
+    case M_LORENZ_ADDNOISE: {
+      du[0] = p[0] * (u[1] - u[0]);
+      du[1] = u[0] * (p[1] - u[2]) - u[1];
+      du[2] = u[0] * u[1] - p[2] * u[2];
+    } break;
+    case M_ROBERTSON: {
+      du[0] = -p[0] * u[0] + p[2] * u[1] * u[2];
+      du[1] = p[0] * u[0] - p[1] * u[1] * u[1] - p[2] * u[1] * u[2];
+      du[2] = p[1] * u[1] * u[1];
+    } break;
+    case M_DECAY: du[0] = -p[0] * u[0]; break;
+    case M_GROWTH: du[0] = u[0]; break;
+    case M_LINEAR15: for (int i = 0; i < 15; i++) du[i] = 1.01f * u[i]; break;
+    case M_GBM: du[0] = p[0] * u[0]; break;
+    case M_OSC: { du[0] = u[1]; du[1] = -(p[0] * p[0]) * u[0]; } break;
+  }
+}
+
+/* analytic Jacobian (column-major J[i + N*j] = d f_i / d u_j) */
+static void model_jac(int m, float* J, const float* u, const float* p, float t) {
+  (void)t;
+  switch (m) {
+    case M_LORENZ:
+      J[0] = -p[0]; J[1] = p[1] - u[2]; J[2] = u[1];
+      J[3] = p[0]; J[4] = -1.0f; J[5] = u[0];
+      J[6] = 0.0f; J[7] = -u[0]; J[8] = -p[2];
+      break;
+    case M_ROBERTSON:
+      J[0] = -p[0]; J[1] = p[0]; J[2] = 0.0f;
+      J[3] = p[2] * u[2]; J[4] = -(p[1] * u[1] + p[1] * u[1]) - p[2] * u[2]; J[5] = p[1] * u[1] + p[1] * u[1];
+      J[6] = p[2] * u[1]; J[7] = -(p[2] * u[1]); J[8] = 0.0f;
+      break;
+    case M_DECAY: J[0] = -p[0]; break;
+    case M_OSC: J[0] = 0.0f; J[1] = -(p[0] * p[0]); J[2] = 1.0f; J[3] = 0.0f; break;
+  }
+}
+static void model_tgrad(int m, float* dT, int N) { (void)m; for (int i = 0; i < N; i++) dT[i] = 0.0f; }
+
+/* SDE noise g (diagonal) */
+static void model_g(int m, float* g, const float* u, const float* p) {
+  switch (m) {
+    case M_GBM: g[0] = p[1] * u[0]; break;
+    case M_LORENZ_ADDNOISE: g[0] = 3.0f; g[1] = 3.0f; g[2] = 3.0f; break;
+  }
+}
+
+/* Jacobian and time-gradient per build_J_W / build_tgrad (nlsolve/type.jl:129-157). */
+static void compute_J(int m, int jacmode, int N, float* J, const float* u, const float* p, float t) {
+  ModelInfo mi = model_info(m);
+  if (jacmode == JAC_ANALYTIC && mi.has_jac) { model_jac(m, J, u, p, t); return; }
+  if (jacmode == JAC_FINITEDIFF) {
+    /* finite_diff_jac, alg_utils.jl:17-27: dx = sqrt(eps(T)), column i = (f(x+dx e_i) - f(x)) / dx */
+    const float dx = sqrtf(1.1920929e-07f);
+    float f0[MAXN], f1[MAXN], x[MAXN];
+    model_f<float>(m, f0, u, p, t);
+    for (int j = 0; j < N; j++) {
+      for (int i = 0; i < N; i++) x[i] = u[i];
+      x[j] = x[j] + dx;
+      model_f<float>(m, f1, x, p, t);
+      for (int i = 0; i < N; i++) J[i + N * j] = (f1[i] - f0[i]) / dx;
+    }
+    return;
+  }
+  /* ForwardDiff.jacobian: one chunk with N partials (N <= MAXN) */
+  Dual<MAXN> ud[MAXN], fd[MAXN];
+  for (int i = 0; i < N; i++) { ud[i] = Dual<MAXN>(u[i]); ud[i].d[i] = 1.0f; }
+  model_f<Dual<MAXN>>(m, fd, ud, p, t);
+  for (int j = 0; j < N; j++)
+    for (int i = 0; i < N; i++) J[i + N * j] = fd[i].d[j];
+}
+static void compute_tgrad(int m, int jacmode, int N, float* dT, const float* u, const float* p, float t) {
+  ModelInfo mi = model_info(m);
+  if (jacmode == JAC_ANALYTIC && mi.has_tgrad) { model_tgrad(m, dT, N); return; }
+  if (jacmode == JAC_FINITEDIFF) {
+    const float h = sqrtf(1.1920929e-07f);
+    float f0[MAXN], f1[MAXN];
+    model_f<float>(m, f1, u, p, t + h);
+    model_f<float>(m, f0, u, p, t);
+    for (int i = 0; i < N; i++) dT[i] = (f1[i] - f0[i]) / h;
+    return;
+  }
+  /* ForwardDiff.derivative w.r.t. t: all built-in models are autonomous */
+  for (int i = 0; i < N; i++) dT[i] = 0.0f;
+}
+
+/* ------------------------------------------------------------------ helpers */
+/* Julia's min/max propagate NaN (Base.min for AbstractFloat) */
+static inline float jl_min(float x, float y) { if (x != x) return x; if (y != y) return y; return y < x ? y : x; }
+static inline float jl_max(float x, float y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
+static inline double jl_mind(double x, double y) { if (x != x) return x; if (y != y) return y; return y < x ? y : x; }
+
+/* DiffEqBase.ODE_DEFAULT_NORM for a static vector: sqrt(sum(abs2, u) / length(u)) */
+static inline float ode_norm(const float* x, int N) {
+  float s = x[0] * x[0];
+  for (int i = 1; i < N; i++) s = s + x[i] * x[i];
+  return sqrtf(s / (float)N);
+}
+
+/* Tsitouras (2011) 5(4) coefficients, as SimpleDiffEq builds them (convert(T, Float64)). */
+struct Tsit5Tab {
+  float c1, c2, c3, c4, c5, c6;
+  float a21, a31, a32, a41, a42, a43, a51, a52, a53, a54, a61, a62, a63, a64, a65, a71, a72, a73, a74, a75, a76;
+  float bt1, bt2, bt3, bt4, bt5, bt6, bt7;
+  float r11, r12, r13, r14, r22, r23, r24, r32, r33, r34, r42, r43, r44, r52, r53, r54, r62, r63, r64, r72, r73, r74;
+};
+static Tsit5Tab make_tsit5() {
+  Tsit5Tab T;
+  T.c1 = (float)0.161; T.c2 = (float)0.327; T.c3 = (float)0.9; T.c4 = (float)0.9800255409045097; T.c5 = 1.0f; T.c6 = 1.0f;
+  T.a21 = (float)0.161;
+  T.a31 = (float)-0.008480655492356989; T.a32 = (float)0.335480655492357;
+  T.a41 = (float)2.897153057105493; T.a42 = (float)-6.359448489975075; T.a43 = (float)4.3622954328695815;
+  T.a51 = (float)5.325864828439257; T.a52 = (float)-11.748883564062828; T.a53 = (float)7.4955393428898365; T.a54 = (float)-0.09249506636175525;
+  T.a61 = (float)5.86145544294642; T.a62 = (float)-12.92096931784711; T.a63 = (float)8.159367898576159; T.a64 = (float)-0.071584973281401; T.a65 = (float)-0.028269050394068383;
+  T.a71 = (float)0.09646076681806523; T.a72 = (float)0.01; T.a73 = (float)0.4798896504144996; T.a74 = (float)1.379008574103742; T.a75 = (float)-3.290069515436081; T.a76 = (float)2.324710524099774;
+  T.bt1 = (float)-0.00178001105222577714; T.bt2 = (float)-0.0008164344596567469; T.bt3 = (float)0.007880878010261995;
+  T.bt4 = (float)-0.1447110071732629; T.bt5 = (float)0.5823571654525552; T.bt6 = (float)-0.45808210592918697; T.bt7 = (float)0.015151515151515152;
+  T.r11 = 1.0f; T.r12 = (float)-2.763706197274826; T.r13 = (float)2.9132554618219126; T.r14 = (float)-1.0530884977290216;
+  T.r22 = (float)0.13169999999999998; T.r23 = (float)-0.2234; T.r24 = (float)0.1017;
+  T.r32 = (float)3.9302962368947516; T.r33 = (float)-5.941033872131505; T.r34 = (float)2.490627285651253;
+  T.r42 = (float)-12.411077166933676; T.r43 = (float)30.33818863028232; T.r44 = (float)-16.548102889244902;
+  T.r52 = (float)37.50931341651104; T.r53 = (float)-88.1789048947664; T.r54 = (float)47.37952196281928;
+  T.r62 = (float)-27.896526289197286; T.r63 = (float)65.09189467479366; T.r64 = (float)-34.87065786149661;
+  T.r72 = 1.5f; T.r73 = -4.0f; T.r74 = 2.5f;
+  return T;
+}
+static const Tsit5Tab TS5 = make_tsit5();
+
+static float V7[OR_VERN7_COUNT], V7X[OR_VERN7X_COUNT], V7I[OR_VERN7I_COUNT], R5P[OR_RODAS5P_COUNT];
+static int tabs_ready = 0;
+static void init_tabs() {
+  if (tabs_ready) return;
+#pragma omp critical(oracle_tabs)
+  {
+    if (!tabs_ready) {
+      for (int i = 0; i < OR_VERN7_COUNT; i++) V7[i] = (float)OR_VERN7[i];
+      for (int i = 0; i < OR_VERN7X_COUNT; i++) V7X[i] = (float)OR_VERN7X[i];
+      for (int i = 0; i < OR_VERN7I_COUNT; i++) V7I[i] = (float)OR_VERN7I[i];
+      for (int i = 0; i < OR_RODAS5P_COUNT; i++) R5P[i] = (float)OR_RODAS5P[i];
+      tabs_ready = 1;
+    }
+  }
+}
+#define V7C(n) V7[OR_VERN7_##n]
+#define V7XC(n) V7X[OR_VERN7X_##n]
+#define V7IC(n) V7I[OR_VERN7I_##n]
+#define RPC(n) R5P[OR_RODAS5P_##n]
+
+/* ------------------------------------------------------------------ configuration */
+extern "C" {
+typedef struct {
+  int alg;             /* ALG_* */
+  int adaptive;        /* 0: vectorized_solve, 1: vectorized_asolve */
+  int time_f64;        /* time type Tt: 0 = Float32 (the reference's Float32 tspan), 1 = Float64 */
+  int save_everystep;
+  int L;               /* saved points per trajectory (output rows) */
+  int nsaveat;         /* 0: no saveat */
+  int saveat_per_traj; /* saveat is [B][nsaveat] instead of [nsaveat] */
+  int jac;             /* JAC_* */
+  const double* saveat;
+  double dt;           /* fixed dt / initial dt (converted to Tt as convert(eltype(tspan), dt)) */
+  float abstol, reltol;
+  long long maxiters;  /* cap on step attempts per trajectory */
+  unsigned long long seed; /* EM: key of the counter-based generator */
+  const float* dt0;    /* optional per-trajectory initial dt (overrides dt) */
+  const float* tolscale; /* optional per-trajectory multiplier of abstol and reltol */
+} oracle_cfg;
+}
+
+/* ------------------------------------------------------------------ integrator state
+ * One struct for all algorithms (the reference's GPU*Integrator structs, types.jl). */
+template <class Tt> struct Integ {
+  int N;
+  float u[MAXN], uprev[MAXN];
+  float k[10][MAXN];      /* Tsit5 k1..k7, Vern7 k1..k10, RB23 k1..k3, Rodas5P dense k1..k3 */
+  float J[MAXN * MAXN], dT[MAXN]; /* Rodas5P: per-step Jacobian (computed once per step) */
+  Tt t, tprev, tf;
+  float dt, dtnew, qold;
+  float abstol, reltol;
+  int u_modified;
+  int cur_t, step_idx;
+  int retcode;
+  long long nattempt, naccept, nreject;
+};
+
+/* time argument handed to f: `t + c*dt` in Tt, passed to the FP32 right-hand side */
+template <class Tt> static inline float tstage(Tt t, float c, float dt) { return (float)(t + (Tt)(c * dt)); }
+
+/* ------------------------------------------------------------------ Tsit5 */
+/* stage block shared by gpu_tsit5_perform_step.jl:36-49 (fixed) and :104-115 (adaptive).
+ * `last6` selects the fixed-step grouping of the final combination (:47-48). */
+template <class Tt>
+static void tsit5_stages(int m, Integ<Tt>& ig, const float* p, Tt t, float dt, const float* k1, float* u, float (*k)[MAXN], int fixed_grouping) {
+  const Tsit5Tab& T = TS5;
+  int N = ig.N;
+  const float* up = ig.uprev;
+  float tmp[MAXN], k2[MAXN], k3[MAXN], k4[MAXN], k5[MAXN], k6[MAXN], k7[MAXN];
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + (dt * T.a21) * k1[i];
+  model_f<float>(m, k2, tmp, p, tstage(t, T.c1, dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (T.a31 * k1[i] + T.a32 * k2[i]);
+  model_f<float>(m, k3, tmp, p, tstage(t, T.c2, dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (T.a41 * k1[i] + T.a42 * k2[i] + T.a43 * k3[i]);
+  model_f<float>(m, k4, tmp, p, tstage(t, T.c3, dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (T.a51 * k1[i] + T.a52 * k2[i] + T.a53 * k3[i] + T.a54 * k4[i]);
+  model_f<float>(m, k5, tmp, p, tstage(t, T.c4, dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (T.a61 * k1[i] + T.a62 * k2[i] + T.a63 * k3[i] + T.a64 * k4[i] + T.a65 * k5[i]);
+  model_f<float>(m, k6, tmp, p, (float)(t + (Tt)dt));
+  for (int i = 0; i < N; i++) {
+    if (fixed_grouping)
+      u[i] = up[i] + dt * ((T.a71 * k1[i] + T.a72 * k2[i] + T.a73 * k3[i] + T.a74 * k4[i]) + T.a75 * k5[i] + T.a76 * k6[i]);
+    else
+      u[i] = up[i] + dt * (T.a71 * k1[i] + T.a72 * k2[i] + T.a73 * k3[i] + T.a74 * k4[i] + T.a75 * k5[i] + T.a76 * k6[i]);
+  }
+  model_f<float>(m, k7, u, p, (float)(t + (Tt)dt));
+  for (int i = 0; i < N; i++) {
+    k[0][i] = k1[i]; k[1][i] = k2[i]; k[2][i] = k3[i]; k[3][i] = k4[i];
+    k[4][i] = k5[i]; k[5][i] = k6[i]; k[6][i] = k7[i];
+  }
+}
+
+/* SimpleDiffEq.bθs: b_iθ by Horner from the highest coefficient */
+static void tsit5_btheta(float th, float* b) {
+  const Tsit5Tab& T = TS5;
+  b[0] = (((T.r14 * th + T.r13) * th + T.r12) * th + T.r11) * th;
+  b[1] = (((T.r24 * th + T.r23) * th + T.r22) * th) * th;
+  b[2] = (((T.r34 * th + T.r33) * th + T.r32) * th) * th;
+  b[3] = (((T.r44 * th + T.r43) * th + T.r42) * th) * th;
+  b[4] = (((T.r54 * th + T.r53) * th + T.r52) * th) * th;
+  b[5] = (((T.r64 * th + T.r63) * th + T.r62) * th) * th;
+  b[6] = (((T.r74 * th + T.r73) * th + T.r72) * th) * th;
+}
+
+/* ------------------------------------------------------------------ Vern7 (k1 recomputed: not FSAL) */
+template <class Tt>
+static void vern7_stages(int m, Integ<Tt>& ig, const float* p, Tt t, float dt, float* u, float (*k)[MAXN]) {
+  int N = ig.N;
+  const float* up = ig.uprev;
+  float tmp[MAXN];
+  float* k1 = k[0]; float* k2 = k[1]; float* k3 = k[2]; float* k4 = k[3]; float* k5 = k[4];
+  float* k6 = k[5]; float* k7 = k[6]; float* k8 = k[7]; float* k9 = k[8]; float* k10 = k[9];
+  model_f<float>(m, k1, up, p, (float)t);
+  float a = dt * V7C(a021);
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + a * k1[i];
+  model_f<float>(m, k2, tmp, p, tstage(t, V7C(c2), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7C(a031) * k1[i] + V7C(a032) * k2[i]);
+  model_f<float>(m, k3, tmp, p, tstage(t, V7C(c3), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7C(a041) * k1[i] + V7C(a043) * k3[i]);
+  model_f<float>(m, k4, tmp, p, tstage(t, V7C(c4), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7C(a051) * k1[i] + V7C(a053) * k3[i] + V7C(a054) * k4[i]);
+  model_f<float>(m, k5, tmp, p, tstage(t, V7C(c5), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7C(a061) * k1[i] + V7C(a063) * k3[i] + V7C(a064) * k4[i] + V7C(a065) * k5[i]);
+  model_f<float>(m, k6, tmp, p, tstage(t, V7C(c6), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7C(a071) * k1[i] + V7C(a073) * k3[i] + V7C(a074) * k4[i] + V7C(a075) * k5[i] + V7C(a076) * k6[i]);
+  model_f<float>(m, k7, tmp, p, tstage(t, V7C(c7), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7C(a081) * k1[i] + V7C(a083) * k3[i] + V7C(a084) * k4[i] + V7C(a085) * k5[i] + V7C(a086) * k6[i] + V7C(a087) * k7[i]);
+  model_f<float>(m, k8, tmp, p, tstage(t, V7C(c8), dt));
+  float g9[MAXN], g10[MAXN];
+  for (int i = 0; i < N; i++) {
+    g9[i] = up[i] + dt * (V7C(a091) * k1[i] + V7C(a093) * k3[i] + V7C(a094) * k4[i] + V7C(a095) * k5[i] + V7C(a096) * k6[i] + V7C(a097) * k7[i] + V7C(a098) * k8[i]);
+    g10[i] = up[i] + dt * (V7C(a101) * k1[i] + V7C(a103) * k3[i] + V7C(a104) * k4[i] + V7C(a105) * k5[i] + V7C(a106) * k6[i] + V7C(a107) * k7[i]);
+  }
+  model_f<float>(m, k9, g9, p, (float)(t + (Tt)dt));
+  model_f<float>(m, k10, g10, p, (float)(t + (Tt)dt));
+  for (int i = 0; i < N; i++)
+    u[i] = up[i] + dt * (V7C(b1) * k1[i] + V7C(b4) * k4[i] + V7C(b5) * k5[i] + V7C(b6) * k6[i] + V7C(b7) * k7[i] + V7C(b8) * k8[i] + V7C(b9) * k9[i]);
+}
+
+/* q_i(Θ) tail-sum polynomials, nonstiff/interpolants.jl:28-88 (Horner, no FMA) */
+static inline float horner6(float th, float a0, float a1, float a2, float a3, float a4, float a5) {
+  return ((((a5 * th + a4) * th + a3) * th + a2) * th + a1) * th + a0;
+}
+static void vern7_q(float th, float* q) {
+#define SYN(II, OUT)                                                       \
+  {                                                                        \
+    float s5 = V7IC(r##II##7), s4 = V7IC(r##II##6) + s5, s3 = V7IC(r##II##5) + s4; \
+    float s2 = V7IC(r##II##4) + s3, s1 = V7IC(r##II##3) + s2;                \
+    OUT = horner6(th, V7IC(r##II##2) + s1, s1, s2, s3, s4, s5);             \
+  }
+  {
+    float s15 = V7IC(r017), s14 = V7IC(r016) + s15, s13 = V7IC(r015) + s14, s12 = V7IC(r014) + s13;
+    float s11 = V7IC(r013) + s12, s10 = V7IC(r012) + s11;
+    q[0] = horner6(th, s10, s11, s12, s13, s14, s15);
+  }
+  SYN(04, q[1]) SYN(05, q[2]) SYN(06, q[3]) SYN(07, q[4]) SYN(08, q[5]) SYN(09, q[6])
+  SYN(11, q[7]) SYN(12, q[8]) SYN(13, q[9]) SYN(14, q[10]) SYN(15, q[11]) SYN(16, q[12])
+#undef SYN
+}
+
+template <class Tt>
+static void vern7_interp(int m, const Integ<Tt>& ig, const float* p, float th, float dt, float* out) {
+  int N = ig.N;
+  const float* up = ig.uprev;
+  const float(*k)[MAXN] = ig.k;
+  float k11[MAXN], k12[MAXN], k13[MAXN], k14[MAXN], k15[MAXN], k16[MAXN], tmp[MAXN];
+  const float *k1 = k[0], *k4 = k[3], *k5 = k[4], *k6 = k[5], *k7 = k[6], *k8 = k[7], *k9 = k[8];
+  Tt tp = ig.tprev;
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7XC(a1101) * k1[i] + V7XC(a1104) * k4[i] + V7XC(a1105) * k5[i] + V7XC(a1106) * k6[i] + V7XC(a1107) * k7[i] + V7XC(a1108) * k8[i] + V7XC(a1109) * k9[i]);
+  model_f<float>(m, k11, tmp, p, tstage(tp, V7XC(c11), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7XC(a1201) * k1[i] + V7XC(a1204) * k4[i] + V7XC(a1205) * k5[i] + V7XC(a1206) * k6[i] + V7XC(a1207) * k7[i] + V7XC(a1208) * k8[i] + V7XC(a1209) * k9[i] + V7XC(a1211) * k11[i]);
+  model_f<float>(m, k12, tmp, p, tstage(tp, V7XC(c12), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7XC(a1301) * k1[i] + V7XC(a1304) * k4[i] + V7XC(a1305) * k5[i] + V7XC(a1306) * k6[i] + V7XC(a1307) * k7[i] + V7XC(a1308) * k8[i] + V7XC(a1309) * k9[i] + V7XC(a1311) * k11[i] + V7XC(a1312) * k12[i]);
+  model_f<float>(m, k13, tmp, p, tstage(tp, V7XC(c13), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7XC(a1401) * k1[i] + V7XC(a1404) * k4[i] + V7XC(a1405) * k5[i] + V7XC(a1406) * k6[i] + V7XC(a1407) * k7[i] + V7XC(a1408) * k8[i] + V7XC(a1409) * k9[i] + V7XC(a1411) * k11[i] + V7XC(a1412) * k12[i] + V7XC(a1413) * k13[i]);
+  model_f<float>(m, k14, tmp, p, tstage(tp, V7XC(c14), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7XC(a1501) * k1[i] + V7XC(a1504) * k4[i] + V7XC(a1505) * k5[i] + V7XC(a1506) * k6[i] + V7XC(a1507) * k7[i] + V7XC(a1508) * k8[i] + V7XC(a1509) * k9[i] + V7XC(a1511) * k11[i] + V7XC(a1512) * k12[i] + V7XC(a1513) * k13[i]);
+  model_f<float>(m, k15, tmp, p, tstage(tp, V7XC(c15), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7XC(a1601) * k1[i] + V7XC(a1604) * k4[i] + V7XC(a1605) * k5[i] + V7XC(a1606) * k6[i] + V7XC(a1607) * k7[i] + V7XC(a1608) * k8[i] + V7XC(a1609) * k9[i] + V7XC(a1611) * k11[i] + V7XC(a1612) * k12[i] + V7XC(a1613) * k13[i]);
+  model_f<float>(m, k16, tmp, p, tstage(tp, V7XC(c16), dt));
+  float q[13];
+  vern7_q(th, q);
+  for (int i = 0; i < N; i++) {
+    float step_sum = dt * (V7C(b1) * k1[i] + V7C(b4) * k4[i] + V7C(b5) * k5[i] + V7C(b6) * k6[i] + V7C(b7) * k7[i] + V7C(b8) * k8[i] + V7C(b9) * k9[i]);
+    float corr = dt * (k1[i] * q[0] + k4[i] * q[1] + k5[i] * q[2] + k6[i] * q[3] + k7[i] * q[4] + k8[i] * q[5] + k9[i] * q[6] +
+                       k11[i] * q[7] + k12[i] * q[8] + k13[i] * q[9] + k14[i] * q[10] + k15[i] * q[11] + k16[i] * q[12]);
+    out[i] = up[i] + th * step_sum + th * (th - 1.0f) * corr;
+  }
+}
+
+/* ------------------------------------------------------------------ linear algebra
+ * linear_solve for N <= 3 (linsolve.jl:8-57): Cramer's rule with StaticArrays' det;
+ * N > 3: partial-pivot LU (lu.jl) + triangular solves. */
+static float det3(const float* a) { /* column-major; det = dot(c1, cross(c2, c3)) */
+  float x0 = a[0], x1 = a[1], x2 = a[2];
+  float y0 = a[3], y1 = a[4], y2 = a[5];
+  float z0 = a[6], z1 = a[7], z2 = a[8];
+  float c0 = y1 * z2 - y2 * z1, c1 = y2 * z0 - y0 * z2, c2 = y0 * z1 - y1 * z0;
+  return x0 * c0 + x1 * c1 + x2 * c2;
+}
+#define A_(i, j) a[(i - 1) + N * (j - 1)]
+static void linear_solve(int N, const float* a, const float* b, float* x) {
+  if (N == 1) { x[0] = b[0] / a[0]; return; }
+  if (N == 2) {
+    float d = a[0] * a[3] - a[2] * a[1];
+    x[0] = (A_(2, 2) * b[0] - A_(1, 2) * b[1]) / d;
+    x[1] = (A_(1, 1) * b[1] - A_(2, 1) * b[0]) / d;
+    return;
+  }
+  if (N == 3) {
+    float d = det3(a);
+    x[0] = ((A_(2, 2) * A_(3, 3) - A_(2, 3) * A_(3, 2)) * b[0] + (A_(1, 3) * A_(3, 2) - A_(1, 2) * A_(3, 3)) * b[1] + (A_(1, 2) * A_(2, 3) - A_(1, 3) * A_(2, 2)) * b[2]) / d;
+    x[1] = ((A_(2, 3) * A_(3, 1) - A_(2, 1) * A_(3, 3)) * b[0] + (A_(1, 1) * A_(3, 3) - A_(1, 3) * A_(3, 1)) * b[1] + (A_(1, 3) * A_(2, 1) - A_(1, 1) * A_(2, 3)) * b[2]) / d;
+    x[2] = ((A_(2, 1) * A_(3, 2) - A_(2, 2) * A_(3, 1)) * b[0] + (A_(1, 2) * A_(3, 1) - A_(1, 1) * A_(3, 2)) * b[1] + (A_(1, 1) * A_(2, 2) - A_(1, 2) * A_(2, 1)) * b[2]) / d;
+    return;
+  }
+  /* partial pivoting LU, row-major working copy */
+  float LU[MAXN][MAXN], y[MAXN];
+  int piv[MAXN];
+  for (int i = 0; i < N; i++) { piv[i] = i; for (int j = 0; j < N; j++) LU[i][j] = a[i + N * j]; }
+  for (int kk = 0; kk < N; kk++) {
+    int pr = kk; float best = fabsf(LU[kk][kk]);
+    for (int i = kk + 1; i < N; i++) if (fabsf(LU[i][kk]) > best) { best = fabsf(LU[i][kk]); pr = i; }
+    if (pr != kk) { for (int j = 0; j < N; j++) { float t = LU[kk][j]; LU[kk][j] = LU[pr][j]; LU[pr][j] = t; } int t = piv[kk]; piv[kk] = piv[pr]; piv[pr] = t; }
+    for (int i = kk + 1; i < N; i++) {
+      LU[i][kk] = LU[i][kk] / LU[kk][kk];
+      for (int j = kk + 1; j < N; j++) LU[i][j] = LU[i][j] - LU[i][kk] * LU[kk][j];
+    }
+  }
+  for (int i = 0; i < N; i++) { float s = b[piv[i]]; for (int j = 0; j < i; j++) s = s - LU[i][j] * y[j]; y[i] = s; }
+  for (int i = N - 1; i >= 0; i--) { float s = y[i]; for (int j = i + 1; j < N; j++) s = s - LU[i][j] * x[j]; x[i] = s / LU[i][i]; }
+}
+#undef A_
+
+/* ------------------------------------------------------------------ controller (integrator_utils.jl:1-11) */
+struct Ctrl { float beta1, beta2, qmax, qmin, gamma, qoldinit; };
+static Ctrl make_ctrl(int order) {
+  Ctrl c;
+  c.beta1 = (float)(7.0 / (10.0 * order));
+  c.beta2 = (float)(2.0 / (5.0 * order));
+  c.qmax = 10.0f; c.qmin = (float)(1.0 / 5.0); c.gamma = (float)(9.0 / 10.0); c.qoldinit = (float)1.0e-4;
+  return c;
+}
+static int alg_order(int alg) { return alg == ALG_TSIT5 ? 5 : alg == ALG_VERN7 ? 7 : alg == ALG_RB23 ? 2 : alg == ALG_RODAS5P ? 5 : 1; }
+
+/* PI controller decision, shared by every adaptive step! (e.g. gpu_tsit5_perform_step.jl:124-170).
+ * Returns 1 if accepted; updates dt (reject) or dt_accepted/dtnew/qold (accept). */
+template <class Tt>
+static int controller(Integ<Tt>& ig, const Ctrl& C, float EEst, float& dt, Tt t) {
+  float q11 = 0.0f, q;
+  if (EEst == 0.0f) q = 1.0f / C.qmax;
+  else { q11 = pm_powf(EEst, C.beta1); q = q11 / pm_powf(ig.qold, C.beta2); }
+  if (EEst > 1.0f) {
+    dt = dt / jl_min(1.0f / C.qmin, q11 / C.gamma);
+    return 0;
+  }
+  q = jl_max(1.0f / C.qmax, jl_min(1.0f / C.qmin, q / C.gamma));
+  ig.qold = jl_max(EEst, C.qoldinit);
+  float dtnew = dt / q;
+  Tt rem = ig.tf - t - (Tt)dt;
+  ig.dtnew = (float)(Tt)jl_mind((double)fabsf(dtnew), fabs((double)rem));
+  ig.dt = dt;
+  ig.tprev = t;
+  if (rem < (Tt)1.0e-14) ig.t = ig.tf;
+  else ig.t = t + (Tt)dt;
+  return 1;
+}
+
+/* error weights: tmp ./ (abstol .+ max.(abs.(uprev), abs.(u)) * reltol) */
+static inline float scaled_norm(const float* e, const float* up, const float* u, int N, float abstol, float reltol) {
+  float tmp[MAXN];
+  for (int i = 0; i < N; i++) tmp[i] = e[i] / (abstol + jl_max(fabsf(up[i]), fabsf(u[i])) * reltol);
+  return ode_norm(tmp, N);
+}
+
+/* ------------------------------------------------------------------ Rosenbrock23 */
+template <class Tt>
+static void rb23_attempt(int m, int jacmode, Integ<Tt>& ig, const float* p, Tt t, float dt, float* u, float* k1o, float* k2o, float* err, int adaptive) {
+  int N = ig.N;
+  const float d = 1.0f / (2.0f + sqrtf(2.0f));
+  float J[MAXN * MAXN], dT[MAXN], W[MAXN * MAXN], F0[MAXN], F1[MAXN], F2[MAXN], rhs[MAXN], tmp[MAXN], k1[MAXN], k2[MAXN], k3[MAXN];
+  float tf_ = (float)t;
+  float gam = dt * d, dto2 = dt / 2.0f, dto6 = dt / 6.0f;
+  compute_J(m, jacmode, N, J, ig.uprev, p, tf_);
+  compute_tgrad(m, jacmode, N, dT, ig.uprev, p, tf_);
+  for (int j = 0; j < N; j++) for (int i = 0; i < N; i++) W[i + N * j] = (i == j ? 1.0f : 0.0f) - gam * J[i + N * j];
+  model_f<float>(m, F0, ig.uprev, p, tf_);
+  for (int i = 0; i < N; i++) rhs[i] = F0[i] + gam * dT[i];
+  linear_solve(N, W, rhs, k1);
+  for (int i = 0; i < N; i++) tmp[i] = ig.uprev[i] + dto2 * k1[i];
+  model_f<float>(m, F1, tmp, p, (float)(t + (Tt)dto2));
+  for (int i = 0; i < N; i++) rhs[i] = F1[i] - k1[i];
+  linear_solve(N, W, rhs, k2);
+  for (int i = 0; i < N; i++) k2[i] = k2[i] + k1[i];
+  for (int i = 0; i < N; i++) u[i] = ig.uprev[i] + dt * k2[i];
+  for (int i = 0; i < N; i++) { k1o[i] = k1[i]; k2o[i] = k2[i]; }
+  if (!adaptive) return;
+  const float e32 = 6.0f + sqrtf(2.0f);
+  model_f<float>(m, F2, u, p, (float)(t + (Tt)dt));
+  for (int i = 0; i < N; i++) rhs[i] = F2[i] - e32 * (k2[i] - F1[i]) - 2.0f * (k1[i] - F0[i]) + dt * dT[i];
+  linear_solve(N, W, rhs, k3);
+  for (int i = 0; i < N; i++) err[i] = dto6 * (k1[i] - 2.0f * k2[i] + k3[i]);
+}
+
+/* ------------------------------------------------------------------ Rodas5P */
+template <class Tt>
+static void rodas5p_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt, float* uout, float* k8o, float (*dense)[MAXN]) {
+  int N = ig.N;
+  const float* J = ig.J; const float* dT = ig.dT; const float* up = ig.uprev;
+  float dtC21 = RPC(C21) / dt, dtC31 = RPC(C31) / dt, dtC32 = RPC(C32) / dt, dtC41 = RPC(C41) / dt, dtC42 = RPC(C42) / dt, dtC43 = RPC(C43) / dt;
+  float dtC51 = RPC(C51) / dt, dtC52 = RPC(C52) / dt, dtC53 = RPC(C53) / dt, dtC54 = RPC(C54) / dt;
+  float dtC61 = RPC(C61) / dt, dtC62 = RPC(C62) / dt, dtC63 = RPC(C63) / dt, dtC64 = RPC(C64) / dt, dtC65 = RPC(C65) / dt;
+  float dtC71 = RPC(C71) / dt, dtC72 = RPC(C72) / dt, dtC73 = RPC(C73) / dt, dtC74 = RPC(C74) / dt, dtC75 = RPC(C75) / dt, dtC76 = RPC(C76) / dt;
+  float dtC81 = RPC(C81) / dt, dtC82 = RPC(C82) / dt, dtC83 = RPC(C83) / dt, dtC84 = RPC(C84) / dt, dtC85 = RPC(C85) / dt, dtC86 = RPC(C86) / dt, dtC87 = RPC(C87) / dt;
+  float dtd1 = dt * RPC(d1), dtd2 = dt * RPC(d2), dtd3 = dt * RPC(d3), dtd4 = dt * RPC(d4), dtd5 = dt * RPC(d5);
+  float dtgamma = dt * RPC(gamma);
+  float W[MAXN * MAXN];
+  float inv_dtg = 1.0f / dtgamma;
+  for (int j = 0; j < N; j++) for (int i = 0; i < N; i++) W[i + N * j] = J[i + N * j] - (i == j ? 1.0f : 0.0f) * inv_dtg;
+  float du[MAXN], u[MAXN], lt[MAXN], neg[MAXN];
+  float k1[MAXN], k2[MAXN], k3[MAXN], k4[MAXN], k5[MAXN], k6[MAXN], k7[MAXN], k8[MAXN];
+  float tf_ = (float)t;
+#define SOLVE(K) { for (int i = 0; i < N; i++) neg[i] = -lt[i]; linear_solve(N, W, neg, K); }
+  model_f<float>(m, du, up, p, tf_);
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd1 * dT[i];
+  SOLVE(k1);
+  for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a21) * k1[i];
+  model_f<float>(m, du, u, p, tstage(t, RPC(c2), dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd2 * dT[i] + dtC21 * k1[i];
+  SOLVE(k2);
+  for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a31) * k1[i] + RPC(a32) * k2[i];
+  model_f<float>(m, du, u, p, tstage(t, RPC(c3), dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd3 * dT[i] + (dtC31 * k1[i] + dtC32 * k2[i]);
+  SOLVE(k3);
+  for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a41) * k1[i] + RPC(a42) * k2[i] + RPC(a43) * k3[i];
+  model_f<float>(m, du, u, p, tstage(t, RPC(c4), dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd4 * dT[i] + (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]);
+  SOLVE(k4);
+  for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a51) * k1[i] + RPC(a52) * k2[i] + RPC(a53) * k3[i] + RPC(a54) * k4[i];
+  model_f<float>(m, du, u, p, tstage(t, RPC(c5), dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd5 * dT[i] + (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]);
+  SOLVE(k5);
+  for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a61) * k1[i] + RPC(a62) * k2[i] + RPC(a63) * k3[i] + RPC(a64) * k4[i] + RPC(a65) * k5[i];
+  model_f<float>(m, du, u, p, (float)(t + (Tt)dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC63 * k3[i] + dtC64 * k4[i] + dtC65 * k5[i]);
+  SOLVE(k6);
+  for (int i = 0; i < N; i++) u[i] = u[i] + k6[i];
+  model_f<float>(m, du, u, p, (float)(t + (Tt)dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC71 * k1[i] + dtC72 * k2[i] + dtC73 * k3[i] + dtC74 * k4[i] + dtC75 * k5[i] + dtC76 * k6[i]);
+  SOLVE(k7);
+  for (int i = 0; i < N; i++) u[i] = u[i] + k7[i];
+  model_f<float>(m, du, u, p, (float)(t + (Tt)dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC81 * k1[i] + dtC82 * k2[i] + dtC83 * k3[i] + dtC84 * k4[i] + dtC85 * k5[i] + dtC86 * k6[i] + dtC87 * k7[i]);
+  SOLVE(k8);
+#undef SOLVE
+  for (int i = 0; i < N; i++) { uout[i] = u[i] + k8[i]; k8o[i] = k8[i]; }
+  for (int i = 0; i < N; i++) {
+    dense[0][i] = RPC(h21) * k1[i] + RPC(h22) * k2[i] + RPC(h23) * k3[i] + RPC(h24) * k4[i] + RPC(h25) * k5[i] + RPC(h26) * k6[i] + RPC(h27) * k7[i] + RPC(h28) * k8[i];
+    dense[1][i] = RPC(h31) * k1[i] + RPC(h32) * k2[i] + RPC(h33) * k3[i] + RPC(h34) * k4[i] + RPC(h35) * k5[i] + RPC(h36) * k6[i] + RPC(h37) * k7[i] + RPC(h38) * k8[i];
+    dense[2][i] = RPC(h41) * k1[i] + RPC(h42) * k2[i] + RPC(h43) * k3[i] + RPC(h44) * k4[i] + RPC(h45) * k5[i] + RPC(h46) * k6[i] + RPC(h47) * k7[i] + RPC(h48) * k8[i];
+  }
+}
+
+/* ------------------------------------------------------------------ interpolation (savevalues!) */
+template <class Tt>
+static void interpolate(int m, int alg, const Integ<Tt>& ig, const float* p, float th, float dt, float* out) {
+  int N = ig.N;
+  const float* y0 = ig.uprev;
+  switch (alg) {
+    case ALG_TSIT5: { /* nonstiff/interpolants.jl:372-387 */
+      float b[7];
+      tsit5_btheta(th, b);
+      for (int i = 0; i < N; i++)
+        out[i] = y0[i] + dt * (b[0] * ig.k[0][i] + b[1] * ig.k[1][i] + b[2] * ig.k[2][i] + b[3] * ig.k[3][i] + b[4] * ig.k[4][i] + b[5] * ig.k[5][i] + b[6] * ig.k[6][i]);
+    } break;
+    case ALG_VERN7: vern7_interp(m, ig, p, th, dt, out); break;
+    case ALG_RB23: { /* nonstiff/interpolants.jl:389-399 */
+      const float d = 1.0f / (2.0f + sqrtf(2.0f));
+      float c1 = th * (1.0f - th) / (1.0f - 2.0f * d);
+      float c2 = th * (th - 2.0f * d) / (1.0f - 2.0f * d);
+      for (int i = 0; i < N; i++) out[i] = y0[i] + dt * (c1 * ig.k[0][i] + c2 * ig.k[1][i]);
+    } break;
+    case ALG_RODAS5P: { /* stiff/interpolants.jl:13-23 */
+      float th1 = 1.0f - th;
+      for (int i = 0; i < N; i++) out[i] = th1 * y0[i] + th * (ig.u[i] + th1 * (ig.k[0][i] + th * (ig.k[1][i] + th * ig.k[2][i])));
+    } break;
+  }
+}
+
+/* ------------------------------------------------------------------ one trajectory (kernels.jl) */
+template <class Tt>
+static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* u0, const float* p, const double* tsp,
+                      Tt* ts, float* us, signed char* retcode, int* nacc, int* nrej) {
+  ModelInfo mi = model_info(m);
+  const int N = mi.N, L = cfg->L, alg = cfg->alg;
+  Integ<Tt> ig;
+  memset(&ig, 0, sizeof(ig));
+  ig.N = N;
+  Tt t0 = (Tt)tsp[0], tf = (Tt)tsp[1];
+  for (int i = 0; i < N; i++) { ig.u[i] = u0[i]; ig.uprev[i] = u0[i]; for (int s = 0; s < 10; s++) ig.k[s][i] = u0[i]; }
+  ig.t = t0; ig.tprev = t0; ig.tf = tf;
+  float dt_in = cfg->dt0 ? cfg->dt0[idx] : (float)(Tt)cfg->dt;
+  ig.dt = dt_in; ig.dtnew = dt_in;
+  float tsc = cfg->tolscale ? cfg->tolscale[idx] : 1.0f;
+  ig.abstol = cfg->abstol * tsc; ig.reltol = cfg->reltol * tsc;
+  ig.u_modified = 1; ig.retcode = RET_DEFAULT;
+  Ctrl C = make_ctrl(alg_order(alg));
+  ig.qold = C.qoldinit;
+
+  /* fill! ts with tspan[1] (lowerlevel_solve.jl:82, 107, 318, 322) */
+  for (int l = 0; l < L; l++) ts[l] = t0;
+  const double* sa = cfg->nsaveat ? (cfg->saveat_per_traj ? cfg->saveat + idx * cfg->nsaveat : cfg->saveat) : NULL;
+  int nsa = cfg->nsaveat;
+#define US(l) (us + (size_t)(l) * N)
+#define SA(l) ((Tt)sa[(l)])
+  /* kernels.jl:35-47 / :116-126 (0-based cur_t here == 1-based cur_t - 1) */
+  ig.cur_t = 0; ig.step_idx = 0;
+  if (sa) {
+    if (t0 == SA(0)) { ig.cur_t = 1; for (int i = 0; i < N; i++) US(0)[i] = u0[i]; }
+  } else {
+    ts[0] = t0; for (int i = 0; i < N; i++) US(0)[i] = u0[i];
+  }
+  ig.step_idx = 1;
+
+  const int save_every = cfg->save_everystep && !cfg->adaptive; /* adaptive init stores save_everystep=false (types.jl) */
+  while (ig.t < tf && ig.retcode != RET_TERMINATED && ig.retcode != RET_DTMIN && ig.retcode != RET_MAXITERS) {
+    /* ---------------- step! ---------------- */
+    Tt t = ig.t;
+    for (int i = 0; i < N; i++) ig.uprev[i] = ig.u[i];
+    if (!cfg->adaptive) {
+      if (++ig.nattempt > cfg->maxiters) { ig.retcode = RET_MAXITERS; break; }
+      float dt = ig.dt;
+      ig.tprev = t;
+      ig.t = t + (Tt)dt;
+      float u[MAXN];
+      if (alg == ALG_TSIT5) {
+        float k1[MAXN];
+        if (ig.u_modified) { model_f<float>(m, k1, ig.uprev, p, (float)t); ig.u_modified = 0; }
+        else for (int i = 0; i < N; i++) k1[i] = ig.k[6][i];
+        tsit5_stages(m, ig, p, t, dt, k1, u, ig.k, 1);
+      } else if (alg == ALG_VERN7) {
+        vern7_stages(m, ig, p, t, dt, u, ig.k);
+      } else if (alg == ALG_RB23) {
+        float err[MAXN];
+        rb23_attempt(m, cfg->jac, ig, p, t, dt, u, ig.k[0], ig.k[1], err, 0);
+      } else if (alg == ALG_RODAS5P) {
+        float k8[MAXN];
+        compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, (float)t);
+        compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, (float)t);
+        rodas5p_attempt(m, ig, p, t, dt, u, k8, ig.k);
+      }
+      for (int i = 0; i < N; i++) ig.u[i] = u[i];
+      ig.naccept++;
+    } else {
+      float dt = ig.dtnew;
+      float k1[MAXN];
+      if (alg == ALG_TSIT5) {
+        if (ig.u_modified) { model_f<float>(m, k1, ig.uprev, p, (float)t); ig.u_modified = 0; }
+        else for (int i = 0; i < N; i++) k1[i] = ig.k[6][i];
+      }
+      if (alg == ALG_RODAS5P) { /* J, dT once per step, outside the reject loop (:182-186) */
+        compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, (float)t);
+        compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, (float)t);
+      }
+      float EEst = INFINITY;
+      while (EEst > 1.0f) {
+        if (dt < 1.0e-14f) { ig.retcode = RET_DTMIN; break; }
+        if (++ig.nattempt > cfg->maxiters) { ig.retcode = RET_MAXITERS; break; }
+        float u[MAXN], err[MAXN], kk[10][MAXN];
+        if (alg == ALG_TSIT5) {
+          tsit5_stages(m, ig, p, t, dt, k1, u, kk, 0);
+          for (int i = 0; i < N; i++)
+            err[i] = dt * (TS5.bt1 * kk[0][i] + TS5.bt2 * kk[1][i] + TS5.bt3 * kk[2][i] + TS5.bt4 * kk[3][i] + TS5.bt5 * kk[4][i] + TS5.bt6 * kk[5][i] + TS5.bt7 * kk[6][i]);
+        } else if (alg == ALG_VERN7) {
+          vern7_stages(m, ig, p, t, dt, u, kk);
+          for (int i = 0; i < N; i++)
+            err[i] = dt * (V7C(btilde1) * kk[0][i] + V7C(btilde4) * kk[3][i] + V7C(btilde5) * kk[4][i] + V7C(btilde6) * kk[5][i] + V7C(btilde7) * kk[6][i] + V7C(btilde8) * kk[7][i] + V7C(btilde9) * kk[8][i] + V7C(btilde10) * kk[9][i]);
+        } else if (alg == ALG_RB23) {
+          rb23_attempt(m, cfg->jac, ig, p, t, dt, u, kk[0], kk[1], err, 1);
+        } else { /* Rodas5P: error estimate is k8 */
+          rodas5p_attempt(m, ig, p, t, dt, u, err, kk);
+        }
+        EEst = scaled_norm(err, ig.uprev, u, N, ig.abstol, ig.reltol);
+        if (controller(ig, C, EEst, dt, t)) {
+          int ns = alg == ALG_TSIT5 ? 7 : alg == ALG_VERN7 ? 10 : alg == ALG_RB23 ? 2 : 3;
+          for (int s = 0; s < ns; s++) for (int i = 0; i < N; i++) ig.k[s][i] = kk[s][i];
+          for (int i = 0; i < N; i++) ig.u[i] = u[i];
+          ig.naccept++;
+        } else {
+          ig.nreject++;
+        }
+      }
+      if (ig.retcode == RET_DTMIN || ig.retcode == RET_MAXITERS) break;
+    }
+    /* ---------------- savevalues! (integrator_utils.jl:13-50) ---------------- */
+    if (!sa && save_every) {
+      if (ig.step_idx < L) { for (int i = 0; i < N; i++) US(ig.step_idx)[i] = ig.u[i]; ts[ig.step_idx] = ig.t; }
+      ig.step_idx++;
+    } else if (sa) {
+      while (ig.cur_t < nsa && SA(ig.cur_t) <= ig.t) {
+        Tt savet = SA(ig.cur_t);
+        float th = (float)((savet - ig.tprev) / (Tt)ig.dt);
+        if (ig.cur_t < L) { interpolate(m, alg, ig, p, th, ig.dt, US(ig.cur_t)); ts[ig.cur_t] = savet; }
+        ig.cur_t++;
+      }
+    }
+  }
+  /* kernels.jl:53-62 / :133-142 */
+  if (ig.t > tf && !sa) {
+    if (!(!cfg->save_everystep)) { /* with !save_everystep slot 2 is overwritten right below */
+      float th = (float)((tf - ig.tprev) / (Tt)ig.dt);
+      interpolate(m, alg, ig, p, th, ig.dt, US(L - 1));
+      ts[L - 1] = tf;
+    }
+  }
+  if (!sa && !cfg->save_everystep) {
+    for (int i = 0; i < N; i++) US(1)[i] = ig.u[i];
+    ts[1] = ig.t;
+  }
+#undef US
+#undef SA
+  int finite = 1;
+  for (int i = 0; i < N; i++) if (!isfinite(ig.u[i])) finite = 0;
+  if (ig.retcode == RET_DEFAULT) ig.retcode = finite ? RET_SUCCESS : RET_UNSTABLE;
+  if (retcode) retcode[idx] = (signed char)ig.retcode;
+  if (nacc) nacc[idx] = (int)ig.naccept;
+  if (nrej) nrej[idx] = (int)ig.nreject;
+}
+
+/* ------------------------------------------------------------------ EM (gpu_em_perform_step.jl:1-74)
+ * Counter-based normals: Philox4x32-10 (Salmon et al., SC'11) keyed by the seed,
+ * counter (step, trajectory, block, 0); Box-Muller with portable log / sincos. */
+static inline uint32_t mulhi32(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) >> 32); }
+static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; r++) {
+    uint32_t hi0 = mulhi32(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    uint32_t hi1 = mulhi32(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+    uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+}
+static void normals4(uint64_t seed, uint32_t step, uint32_t traj, uint32_t blk, float* z) {
+  uint32_t c[4] = {step, traj, blk, 0u};
+  philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  for (int h = 0; h < 2; h++) {
+    float u1 = (float)((c[2 * h] >> 8) + 1u) * 5.9604645e-08f;  /* (0, 1] */
+    float u2 = (float)(c[2 * h + 1] >> 8) * 5.9604645e-08f;     /* [0, 1) */
+    float r = sqrtf(-2.0f * pm_logf(u1));
+    float s, co;
+    pm_sincos_turns(u2, &s, &co);
+    z[2 * h] = r * co; z[2 * h + 1] = r * s;
+  }
+}
+
+template <class Tt>
+static void em_one(int m, const oracle_cfg* cfg, long long idx, const float* u0, const float* p, const double* tsp, Tt* ts, float* us, signed char* retcode) {
+  ModelInfo mi = model_info(m);
+  const int N = mi.N, L = cfg->L;
+  Tt t0 = (Tt)tsp[0], tf = (Tt)tsp[1];
+  Tt dtT = (Tt)cfg->dt;
+  float dt = (float)dtT;
+  for (int l = 0; l < L; l++) ts[l] = t0;
+  const double* sa = cfg->nsaveat ? (cfg->saveat_per_traj ? cfg->saveat + idx * cfg->nsaveat : cfg->saveat) : NULL;
+  int nsa = cfg->nsaveat, cur_t = 0;
+#define US(l) (us + (size_t)(l) * N)
+  if (sa) { if (t0 == (Tt)sa[0]) { cur_t = 1; for (int i = 0; i < N; i++) US(0)[i] = u0[i]; } }
+  else { ts[0] = t0; for (int i = 0; i < N; i++) US(0)[i] = u0[i]; }
+  float sqdt = sqrtf(dt);
+  float u[MAXN], up[MAXN], f[MAXN], g[MAXN], z[MAXN + 4];
+  for (int i = 0; i < N; i++) u[i] = u0[i];
+  Tt t = t0;
+  Tt span = tf - t0;
+  Tt ratio = (span < 0 ? -span : span) / (dtT < 0 ? -dtT : dtT); /* floor(Int, abs(tf - t0) / abs(dt)) in Tt */
+  long long n = (long long)floor((double)ratio) + 1;
+  if (n - 1 > cfg->maxiters) n = cfg->maxiters + 1;
+  for (long long j = 2; j <= n; j++) {
+    for (int i = 0; i < N; i++) up[i] = u[i];
+    model_f<float>(m, f, up, p, (float)t);
+    model_g(m, g, up, p);
+    for (int b = 0; b < (N + 3) / 4; b++) normals4(cfg->seed, (uint32_t)(j - 2), (uint32_t)idx, (uint32_t)b, z + 4 * b);
+    for (int i = 0; i < N; i++) u[i] = up[i] + f[i] * dt + (sqdt * g[i]) * z[i];
+    t = t + (Tt)dt;
+    if (!sa && cfg->save_everystep) {
+      if (j - 1 < L) { for (int i = 0; i < N; i++) US(j - 1)[i] = u[i]; ts[j - 1] = t; }
+    } else if (sa) {
+      while (cur_t < nsa && (Tt)sa[cur_t] <= t) {
+        Tt savet = (Tt)sa[cur_t];
+        float th = (float)((savet - (t - (Tt)dt)) / (Tt)dt);
+        if (cur_t < L) { for (int i = 0; i < N; i++) US(cur_t)[i] = up[i] + (u[i] - up[i]) * th; ts[cur_t] = savet; }
+        cur_t++;
+      }
+    }
+  }
+  if (!sa && !cfg->save_everystep) { for (int i = 0; i < N; i++) US(1)[i] = u[i]; ts[1] = t; }
+#undef US
+  int finite = 1;
+  for (int i = 0; i < N; i++) if (!isfinite(u[i])) finite = 0;
+  if (retcode) retcode[idx] = finite ? RET_SUCCESS : RET_UNSTABLE;
+}
+
+/* ------------------------------------------------------------------ public C API */
+extern "C" {
+
+int oracle_model_dims(int model, int* N, int* P) {
+  ModelInfo mi = model_info(model);
+  if (!mi.N) return -1;
+  *N = mi.N; *P = mi.P;
+  return 0;
+}
+
+/* Ensemble solve on the host cores.  Layouts match the library's: u0 [B][N], p [B][P],
+ * tspan [B][2] (f64, converted to Tt), ts [B][L] (Tt), us [B][L][N] (f32). */
+int oracle_solve(int model, long long B, const float* u0, const float* p, const double* tspan,
+                 const oracle_cfg* cfg, void* ts, float* us, signed char* retcode, int* naccept, int* nreject,
+                 int nthreads) {
+  ModelInfo mi = model_info(model);
+  if (!mi.N || B < 0 || cfg->L < 1) return -1;
+  if (!cfg->adaptive && !cfg->nsaveat && !cfg->save_everystep && cfg->L != 2) return -2;
+  init_tabs();
+  const int N = mi.N, P = mi.P, L = cfg->L;
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+  for (long long i = 0; i < B; i++) {
+    const float* pi = p + (size_t)i * P;
+    const double* tsp = tspan + 2 * (size_t)i;
+    float* usi = us + (size_t)i * L * N;
+    if (cfg->alg == ALG_EM) {
+      if (cfg->time_f64) em_one<double>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (double*)ts + (size_t)i * L, usi, retcode);
+      else em_one<float>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (float*)ts + (size_t)i * L, usi, retcode);
+    } else {
+      if (cfg->time_f64) solve_one<double>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (double*)ts + (size_t)i * L, usi, retcode, naccept, nreject);
+      else solve_one<float>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (float*)ts + (size_t)i * L, usi, retcode, naccept, nreject);
+    }
+  }
+  return 0;
+}
+
+/* the portable math used by parity mode, exported so tests can check its accuracy */
+float oracle_pm_powf(float x, float y) { return pm_powf(x, y); }
+float oracle_pm_logf(float x) { return pm_logf(x); }
+float oracle_pm_expf(float x) { return pm_expf(x); }
+void oracle_normals4(unsigned long long seed, unsigned step, unsigned traj, unsigned blk, float* z) { normals4(seed, step, traj, blk, z); }
+
+/* ------------------------------------------------------------------ FP64 Vern9 error oracle
+ * Explicit 16-stage Verner 9(8) pair (tableaus/verner_tableaus.jl:1198-1332), generic
+ * stage loop, standard PI-free controller with safety 0.9; saves land exactly on the
+ * requested times (the step is clipped), so no interpolation error enters the oracle. */
+static double V9A[17][17], V9C[17], V9B[17], V9BT[17];
+static int v9_ready = 0;
+static void init_v9() {
+  if (v9_ready) return;
+#pragma omp critical(oracle_v9)
+  if (!v9_ready) {
+    memset(V9A, 0, sizeof(V9A)); memset(V9C, 0, sizeof(V9C)); memset(V9B, 0, sizeof(V9B)); memset(V9BT, 0, sizeof(V9BT));
+#define AV(r, c, n) V9A[r][c] = OR_VERN9[OR_VERN9_##n];
+    AV(2, 1, a0201) AV(3, 1, a0301) AV(3, 2, a0302) AV(4, 1, a0401) AV(4, 3, a0403) AV(5, 1, a0501) AV(5, 3, a0503) AV(5, 4, a0504)
+    AV(6, 1, a0601) AV(6, 4, a0604) AV(6, 5, a0605) AV(7, 1, a0701) AV(7, 4, a0704) AV(7, 5, a0705) AV(7, 6, a0706)
+    AV(8, 1, a0801) AV(8, 6, a0806) AV(8, 7, a0807) AV(9, 1, a0901) AV(9, 6, a0906) AV(9, 7, a0907) AV(9, 8, a0908)
+    AV(10, 1, a1001) AV(10, 6, a1006) AV(10, 7, a1007) AV(10, 8, a1008) AV(10, 9, a1009)
+    AV(11, 1, a1101) AV(11, 6, a1106) AV(11, 7, a1107) AV(11, 8, a1108) AV(11, 9, a1109) AV(11, 10, a1110)
+    AV(12, 1, a1201) AV(12, 6, a1206) AV(12, 7, a1207) AV(12, 8, a1208) AV(12, 9, a1209) AV(12, 10, a1210) AV(12, 11, a1211)
+    AV(13, 1, a1301) AV(13, 6, a1306) AV(13, 7, a1307) AV(13, 8, a1308) AV(13, 9, a1309) AV(13, 10, a1310) AV(13, 11, a1311) AV(13, 12, a1312)
+    AV(14, 1, a1401) AV(14, 6, a1406) AV(14, 7, a1407) AV(14, 8, a1408) AV(14, 9, a1409) AV(14, 10, a1410) AV(14, 11, a1411) AV(14, 12, a1412) AV(14, 13, a1413)
+    AV(15, 1, a1501) AV(15, 6, a1506) AV(15, 7, a1507) AV(15, 8, a1508) AV(15, 9, a1509) AV(15, 10, a1510) AV(15, 11, a1511) AV(15, 12, a1512) AV(15, 13, a1513) AV(15, 14, a1514)
+    AV(16, 1, a1601) AV(16, 6, a1606) AV(16, 7, a1607) AV(16, 8, a1608) AV(16, 9, a1609) AV(16, 10, a1610) AV(16, 11, a1611) AV(16, 12, a1612) AV(16, 13, a1613)
+#undef AV
+#define CV(s, n) V9C[s] = OR_VERN9[OR_VERN9_##n];
+    CV(2, c1) CV(3, c2) CV(4, c3) CV(5, c4) CV(6, c5) CV(7, c6) CV(8, c7) CV(9, c8) CV(10, c9) CV(11, c10) CV(12, c11) CV(13, c12) CV(14, c13)
+#undef CV
+    V9C[15] = 1.0; V9C[16] = 1.0;
+#define BV(s, n) V9B[s] = OR_VERN9[OR_VERN9_##n];
+    BV(1, b1) BV(8, b8) BV(9, b9) BV(10, b10) BV(11, b11) BV(12, b12) BV(13, b13) BV(14, b14) BV(15, b15)
+#undef BV
+#define BT(s, n) V9BT[s] = OR_VERN9[OR_VERN9_##n];
+    BT(1, btilde1) BT(8, btilde8) BT(9, btilde9) BT(10, btilde10) BT(11, btilde11) BT(12, btilde12) BT(13, btilde13) BT(14, btilde14) BT(15, btilde15) BT(16, btilde16)
+#undef BT
+    v9_ready = 1;
+  }
+}
+
+static void f64_rhs(int m, double* du, const double* u, const double* p, double t) {
+  (void)t;
+  switch (m) {
+    case M_LORENZ: case M_LORENZ_ADDNOISE:
+      du[0] = p[0] * (u[1] - u[0]); du[1] = u[0] * (p[1] - u[2]) - u[1]; du[2] = u[0] * u[1] - p[2] * u[2]; break;
+    case M_ROBERTSON:
+      du[0] = -p[0] * u[0] + p[2] * u[1] * u[2]; du[1] = p[0] * u[0] - p[1] * u[1] * u[1] - p[2] * u[1] * u[2]; du[2] = p[1] * u[1] * u[1]; break;
+    case M_DECAY: du[0] = -p[0] * u[0]; break;
+    case M_GROWTH: du[0] = u[0]; break;
+    case M_LINEAR15: for (int i = 0; i < 15; i++) du[i] = 1.01 * u[i]; break;
+    case M_GBM: du[0] = p[0] * u[0]; break;
+    case M_OSC: du[0] = u[1]; du[1] = -(p[0] * p[0]) * u[0]; break;
+  }
+}
+
+/* Integrate one trajectory from t0 through the increasing times `stops` (the last is tf);
+ * writes the state at each stop.  Returns the number of accepted steps, or -1. */
+static long long vern9_traj(int m, int N, const double* u0, const double* p, double t0, int nstop, const double* stops,
+                            double rtol, double atol, double* out, long long maxsteps) {
+  double u[MAXN], k[17][MAXN], y[MAXN], un[MAXN];
+  for (int i = 0; i < N; i++) u[i] = u0[i];
+  double t = t0, h = 1e-3 * (stops[nstop - 1] - t0 > 0 ? 1.0 : 1.0);
+  if (nstop > 0 && stops[nstop - 1] - t0 > 0 && h > stops[nstop - 1] - t0) h = stops[nstop - 1] - t0;
+  long long nacc = 0, tries = 0;
+  int si = 0;
+  while (si < nstop && stops[si] <= t) { for (int i = 0; i < N; i++) out[si * N + i] = u[i]; si++; }
+  while (si < nstop) {
+    if (++tries > maxsteps) return -1;
+    double target = stops[si];
+    int land = 0;
+    double hh = h;
+    if (t + hh >= target) { hh = target - t; land = 1; }
+    f64_rhs(m, k[1], u, p, t);
+    for (int s = 2; s <= 16; s++) {
+      for (int i = 0; i < N; i++) { double acc = 0.0; for (int j = 1; j < s; j++) acc += V9A[s][j] * k[j][i]; y[i] = u[i] + hh * acc; }
+      f64_rhs(m, k[s], y, p, t + V9C[s] * hh);
+    }
+    double err = 0.0;
+    for (int i = 0; i < N; i++) {
+      double acc = 0.0, ea = 0.0;
+      for (int s = 1; s <= 16; s++) { acc += V9B[s] * k[s][i]; ea += V9BT[s] * k[s][i]; }
+      un[i] = u[i] + hh * acc;
+      double sc = atol + rtol * fmax(fabs(u[i]), fabs(un[i]));
+      double e = hh * ea / sc;
+      err += e * e;
+    }
+    err = sqrt(err / N);
+    if (!(err == err)) return -1;
+    if (err <= 1.0) {
+      for (int i = 0; i < N; i++) u[i] = un[i];
+      t = land ? target : t + hh;
+      nacc++;
+      while (si < nstop && stops[si] <= t) { for (int i = 0; i < N; i++) out[si * N + i] = u[i]; si++; }
+      double fac = err == 0.0 ? 5.0 : fmin(5.0, fmax(0.2, 0.9 * pow(err, -1.0 / 9.0)));
+      if (!land || hh >= h) h = hh * fac; /* a clipped landing step does not shrink h */
+    } else {
+      h = hh * fmax(0.2, 0.9 * pow(err, -1.0 / 9.0));
+    }
+    if (h < 1e-15) return -1;
+  }
+  return nacc;
+}
+
+/* FP64 reference solutions.  stops: shared [nstop] (per_traj=0) or [B][nstop] (per_traj=1);
+ * out [B][nstop][N].  Returns the number of trajectories that failed. */
+long long oracle_vern9_f64(int model, long long B, const double* u0, const double* p, const double* t0,
+                           int nstop, const double* stops, int per_traj, double rtol, double atol,
+                           double* out, long long* nsteps, int nthreads) {
+  ModelInfo mi = model_info(model);
+  if (!mi.N) return -1;
+  init_v9();
+  const int N = mi.N, P = mi.P;
+  long long fails = 0;
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : fails)
+  for (long long i = 0; i < B; i++) {
+    const double* st = per_traj ? stops + (size_t)i * nstop : stops;
+    long long r = vern9_traj(model, N, u0 + (size_t)i * N, p + (size_t)i * P, t0[i], nstop, st, rtol, atol,
+                             out + (size_t)i * nstop * N, 50000000LL);
+    if (nsteps) nsteps[i] = r;
+    if (r < 0) fails++;
+  }
+  return fails;
+}
+
+/* ------------------------------------------------------------------ FP64 stiff error oracle
+ * An explicit Vern9 would need ~1e12 steps on Robertson over (0, 1e5), so stiff problems
+ * are checked against FP64 Rodas5P (tableau rodas_tableaus.jl:186-283) with partial-pivot
+ * LU, the analytic Jacobian and tight tolerances; tests cross-check it with scipy Radau. */
+static void f64_jac(int m, double* J, const double* u, const double* p) {
+  switch (m) {
+    case M_ROBERTSON:
+      J[0] = -p[0]; J[1] = p[0]; J[2] = 0.0;
+      J[3] = p[2] * u[2]; J[4] = -2.0 * p[1] * u[1] - p[2] * u[2]; J[5] = 2.0 * p[1] * u[1];
+      J[6] = p[2] * u[1]; J[7] = -p[2] * u[1]; J[8] = 0.0;
+      break;
+    case M_LORENZ: case M_LORENZ_ADDNOISE:
+      J[0] = -p[0]; J[1] = p[1] - u[2]; J[2] = u[1]; J[3] = p[0]; J[4] = -1.0; J[5] = u[0]; J[6] = 0.0; J[7] = -u[0]; J[8] = -p[2];
+      break;
+    case M_DECAY: J[0] = -p[0]; break;
+    case M_GROWTH: J[0] = 1.0; break;
+    case M_OSC: J[0] = 0.0; J[1] = -(p[0] * p[0]); J[2] = 1.0; J[3] = 0.0; break;
+    case M_LINEAR15: for (int i = 0; i < 225; i++) J[i] = 0.0; for (int i = 0; i < 15; i++) J[i * 16] = 1.01; break;
+    case M_GBM: J[0] = p[0]; break;
+  }
+}
+static void lu_f64(int N, double* A, int* piv) { /* column-major in place */
+  for (int k = 0; k < N; k++) {
+    int pr = k; double best = fabs(A[k + N * k]);
+    for (int i = k + 1; i < N; i++) if (fabs(A[i + N * k]) > best) { best = fabs(A[i + N * k]); pr = i; }
+    piv[k] = pr;
+    if (pr != k) for (int j = 0; j < N; j++) { double t = A[k + N * j]; A[k + N * j] = A[pr + N * j]; A[pr + N * j] = t; }
+    for (int i = k + 1; i < N; i++) {
+      A[i + N * k] /= A[k + N * k];
+      for (int j = k + 1; j < N; j++) A[i + N * j] -= A[i + N * k] * A[k + N * j];
+    }
+  }
+}
+static void lus_f64(int N, const double* A, const int* piv, double* b) {
+  for (int k = 0; k < N; k++) if (piv[k] != k) { double t = b[k]; b[k] = b[piv[k]]; b[piv[k]] = t; }
+  for (int i = 0; i < N; i++) for (int j = 0; j < i; j++) b[i] -= A[i + N * j] * b[j];
+  for (int i = N - 1; i >= 0; i--) { for (int j = i + 1; j < N; j++) b[i] -= A[i + N * j] * b[j]; b[i] /= A[i + N * i]; }
+}
+static long long rodas5p_f64_traj(int m, int N, const double* u0, const double* p, double t0, int nstop, const double* stops,
+                                  double rtol, double atol, double* out, long long maxsteps) {
+#define R(n) OR_RODAS5P[OR_RODAS5P_##n]
+  const double a[6][6] = {{0}, {R(a21)}, {R(a31), R(a32)}, {R(a41), R(a42), R(a43)}, {R(a51), R(a52), R(a53), R(a54)}, {R(a61), R(a62), R(a63), R(a64), R(a65)}};
+  const double C[8][8] = {{0}, {R(C21)}, {R(C31), R(C32)}, {R(C41), R(C42), R(C43)}, {R(C51), R(C52), R(C53), R(C54)},
+                          {R(C61), R(C62), R(C63), R(C64), R(C65)}, {R(C71), R(C72), R(C73), R(C74), R(C75), R(C76)},
+                          {R(C81), R(C82), R(C83), R(C84), R(C85), R(C86), R(C87)}};
+  const double cc[6] = {0.0, R(c2), R(c3), R(c4), R(c5), 1.0};
+  const double dd[6] = {R(d1), R(d2), R(d3), R(d4), R(d5), 0.0};
+  const double gam = R(gamma);
+#undef R
+  double u[MAXN], J[MAXN * MAXN], W[MAXN * MAXN], k[8][MAXN], du[MAXN], y[MAXN];
+  int piv[MAXN];
+  for (int i = 0; i < N; i++) u[i] = u0[i];
+  double t = t0, h = 1e-8;
+  long long nacc = 0, tries = 0;
+  int si = 0;
+  while (si < nstop && stops[si] <= t) { for (int i = 0; i < N; i++) out[si * N + i] = u[i]; si++; }
+  while (si < nstop) {
+    if (++tries > maxsteps) return -1;
+    double target = stops[si];
+    int land = 0;
+    double hh = h;
+    if (t + hh >= target) { hh = target - t; land = 1; }
+    f64_jac(m, J, u, p);
+    for (int j = 0; j < N; j++) for (int i = 0; i < N; i++) W[i + N * j] = J[i + N * j] - (i == j ? 1.0 / (hh * gam) : 0.0);
+    lu_f64(N, W, piv);
+    for (int s = 0; s < 8; s++) {
+      if (s < 6) for (int i = 0; i < N; i++) { double acc = u[i]; for (int j = 0; j < s; j++) acc += a[s][j] * k[j][i]; y[i] = acc; }
+      else for (int i = 0; i < N; i++) y[i] = y[i] + k[s - 1][i];
+      f64_rhs(m, du, y, p, t + (s < 6 ? cc[s] : 1.0) * hh);
+      for (int i = 0; i < N; i++) {
+        double acc = du[i] + (s < 5 ? dd[s] * hh * 0.0 : 0.0); /* autonomous models: dT = 0 */
+        for (int j = 0; j < s; j++) acc += C[s][j] / hh * k[j][i];
+        k[s][i] = -acc;
+      }
+      lus_f64(N, W, piv, k[s]);
+    }
+    double err = 0.0, un[MAXN];
+    for (int i = 0; i < N; i++) {
+      un[i] = y[i] + k[7][i];
+      double sc = atol + rtol * fmax(fabs(u[i]), fabs(un[i]));
+      err += (k[7][i] / sc) * (k[7][i] / sc);
+    }
+    err = sqrt(err / N);
+    if (!(err == err)) { h = hh * 0.2; continue; }
+    if (err <= 1.0) {
+      for (int i = 0; i < N; i++) u[i] = un[i];
+      t = land ? target : t + hh;
+      nacc++;
+      while (si < nstop && stops[si] <= t) { for (int i = 0; i < N; i++) out[si * N + i] = u[i]; si++; }
+      double fac = err == 0.0 ? 5.0 : fmin(5.0, fmax(0.2, 0.9 * pow(err, -1.0 / 5.0)));
+      if (!land || hh >= h) h = hh * fac;
+    } else {
+      h = hh * fmax(0.2, 0.9 * pow(err, -1.0 / 5.0));
+    }
+    if (h < 1e-18) return -1;
+  }
+  return nacc;
+}
+
+long long oracle_rodas5p_f64(int model, long long B, const double* u0, const double* p, const double* t0,
+                             int nstop, const double* stops, int per_traj, double rtol, double atol,
+                             double* out, long long* nsteps, int nthreads) {
+  ModelInfo mi = model_info(model);
+  if (!mi.N) return -1;
+  const int N = mi.N, P = mi.P;
+  long long fails = 0;
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : fails)
+  for (long long i = 0; i < B; i++) {
+    const double* st = per_traj ? stops + (size_t)i * nstop : stops;
+    long long r = rodas5p_f64_traj(model, N, u0 + (size_t)i * N, p + (size_t)i * P, t0[i], nstop, st, rtol, atol,
+                                   out + (size_t)i * nstop * N, 50000000LL);
+    if (nsteps) nsteps[i] = r;
+    if (r < 0) fails++;
+  }
+  return fails;
+}
+
+} /* extern "C" */
