@@ -880,6 +880,11 @@ int oracle_solve(int model, long long B, const float* u0, const float* p, const 
 float oracle_pm_powf(float x, float y) { return pm_powf(x, y); }
 float oracle_pm_logf(float x) { return pm_logf(x); }
 float oracle_pm_expf(float x) { return pm_expf(x); }
+void oracle_philox4x32_10(const unsigned* ctr, unsigned k0, unsigned k1, unsigned* out) {
+  uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  philox4x32_10(c, k0, k1);
+  for (int i = 0; i < 4; i++) out[i] = c[i];
+}
 void oracle_normals4(unsigned long long seed, unsigned step, unsigned traj, unsigned blk, float* z) { normals4(seed, step, traj, blk, z); }
 
 /* ------------------------------------------------------------------ FP64 Vern9 error oracle

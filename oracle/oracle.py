@@ -69,6 +69,7 @@ def lib():
         L.oracle_pm_logf.argtypes = [ctypes.c_float]
         L.oracle_pm_expf.argtypes = [ctypes.c_float]
         L.oracle_normals4.argtypes = [ctypes.c_ulonglong, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p]
+        L.oracle_philox4x32_10.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p]
         L.oracle_model_dims.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         _lib = L
     return _lib
@@ -162,6 +163,13 @@ def normals4(seed: int, step: int, traj: int, blk: int):
     z = np.zeros(4, dtype=np.float32)
     lib().oracle_normals4(seed, step, traj, blk, _ptr(z))
     return z
+
+
+def philox(ctr, key):
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib().oracle_philox4x32_10(_ptr(c), int(key[0]), int(key[1]), _ptr(out))
+    return out
 
 
 def pm_powf(x: float, y: float) -> float:

@@ -1,0 +1,305 @@
+"""Pinning the CPU oracle (no GPU): method coefficients, FP64 oracles against scipy,
+known answers, empirical orders, the reference's own regression tolerances, the
+Philox known-answer vectors and the portable math used by parity mode."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+# ----------------------------------------------------------------------------- coefficients
+def tsit5_fp64():
+    """The FP64 literals of the oracle's Tsit5 table (make_tsit5 in oracle/oracle.cpp)."""
+    src = (ROOT / "oracle" / "oracle.cpp").read_text()
+    body = src[src.index("static Tsit5Tab make_tsit5()"):src.index("static const Tsit5Tab TS5")]
+    vals = {}
+    for name, lit in re.findall(r"T\.(\w+) = (?:\(float\))?(-?[0-9.eE+-]+)f?;", body):
+        vals[name] = float(lit)
+    return vals
+
+
+def test_tsit5_order_conditions():
+    """Tsitouras (2011) 5(4): all 17 order-5 conditions of b, the 8 order-4 conditions of
+    the embedded b - btilde, and b(theta=1) = b for the dense output (FP64, < 1e-14)."""
+    T = tsit5_fp64()
+    c = np.array([0, T["c1"], T["c2"], T["c3"], T["c4"], 1.0, 1.0])
+    A = np.zeros((7, 7))
+    for i in range(2, 8):
+        for j in range(1, i):
+            A[i - 1, j - 1] = T[f"a{i}{j}"]
+    b = A[6].copy()
+    bt = np.array([T[f"bt{i}"] for i in range(1, 8)])
+    assert np.abs(A.sum(1) - c).max() < 1e-14
+
+    def resid(b, order):
+        r = [b.sum() - 1, b @ c - 1 / 2, b @ c**2 - 1 / 3, b @ A @ c - 1 / 6]
+        r += [b @ c**3 - 1 / 4, b @ (c * (A @ c)) - 1 / 8, b @ A @ c**2 - 1 / 12, b @ A @ A @ c - 1 / 24]
+        if order >= 5:
+            r += [b @ c**4 - 1 / 5, b @ (c**2 * (A @ c)) - 1 / 10, b @ ((A @ c) ** 2) - 1 / 20,
+                  b @ (c * (A @ c**2)) - 1 / 15, b @ (c * (A @ A @ c)) - 1 / 30, b @ A @ c**3 - 1 / 20,
+                  b @ A @ (c * (A @ c)) - 1 / 40, b @ A @ A @ c**2 - 1 / 60, b @ A @ A @ A @ c - 1 / 120]
+        return np.abs(r).max()
+    assert resid(b, 5) < 1e-14
+    assert resid(b - bt, 4) < 1e-14
+    assert resid(b - bt, 5) > 1e-5  # the embedded method really is of lower order
+    r = lambda i, k: T.get(f"r{i}{k}", 0.0)
+    th = 1.0
+    b1 = np.array([r(1, 1) * th + r(1, 2) * th**2 + r(1, 3) * th**3 + r(1, 4) * th**4] +
+                  [r(i, 2) * th**2 + r(i, 3) * th**3 + r(i, 4) * th**4 for i in range(2, 8)])
+    assert np.abs(b1 - b).max() < 1e-14
+
+
+def test_kernel_tsit5_table_matches_oracle():
+    """The kernels' constant-memory Tsit5 table holds the same FP64 literals as the oracle."""
+    dev = (ROOT / "diffeqgpu.jl_gb300" / "csrc" / "device" / "degpu_kernels.cuh").read_text()
+    block = dev[dev.index("__constant__ float c_tsit5[TS_COUNT]"):]
+    block = block[:block.index("};")]
+    lits = [float(x) for x in re.findall(r"\(float\)(-?[0-9.eE+-]+)|(-?[0-9.]+)f", block) for x in x if x]
+    T = tsit5_fp64()
+    order = ["c1", "c2", "c3", "c4"] + [f"a{i}{j}" for i in range(2, 8) for j in range(1, i)] + \
+            [f"bt{i}" for i in range(1, 8)] + ["r11", "r12", "r13", "r14"] + \
+            [f"r{i}{k}" for i in range(2, 8) for k in (2, 3, 4)]
+    assert len(lits) == len(order)
+    for name, v in zip(order, lits):
+        assert np.float32(v) == np.float32(T[name]), name
+
+
+def parse_tab(name):
+    src = (ROOT / "oracle" / "tableaus_gen.h").read_text()
+    block = src[src.index(f"static const double OR_{name}["):]
+    block = block[:block.index("};")]
+    return {n: float(v) for v, n in re.findall(r"(-?[0-9.eE+-]+), /\* (\w+) \*/", block)}
+
+
+def test_generated_tables_consistent():
+    """Device and oracle tables were generated together: same names, FP32 of the same FP64."""
+    dev = (ROOT / "diffeqgpu.jl_gb300" / "csrc" / "device" / "tableaus_gen.cuh").read_text()
+    for tab in ("VERN7", "VERN7X", "VERN7I", "RODAS5P"):
+        fp64 = parse_tab(tab)
+        block = dev[dev.index(f"__constant__ float c_{tab.lower()}["):]
+        block = block[:block.index("};")]
+        vals = re.findall(r"(-?[0-9.eE+-]+)f, // (\w+)", block)
+        assert [n for _, n in vals] == list(fp64)
+        for v, n in vals:
+            assert np.float32(float(v)) == np.float32(fp64[n]), (tab, n)
+
+
+def _verner_conditions(T, stages, cnames, amap, bnames, btnames, order):
+    """Quadrature + row-sum conditions of an explicit RK pair given by name maps."""
+    s = stages
+    c = np.zeros(s)
+    A = np.zeros((s, s))
+    for (i, j), n in amap.items():
+        A[i - 1, j - 1] = T[n]
+    for i, n in cnames.items():
+        c[i - 1] = T[n] if isinstance(n, str) else n
+    b = np.zeros(s)
+    for i, n in bnames.items():
+        b[i - 1] = T[n]
+    bt = np.zeros(s)
+    for i, n in btnames.items():
+        bt[i - 1] = T[n]
+    rows = np.abs(A.sum(1) - c).max()
+    quad = max(abs(b @ c**k - 1 / (k + 1)) for k in range(order))
+    quad_hat = max(abs((b - bt) @ c**k - 1 / (k + 1)) for k in range(order - 1))
+    return rows, quad, quad_hat, A, b, c
+
+
+def test_vern7_and_vern9_quadrature_conditions():
+    T7 = parse_tab("VERN7")
+    amap = {(int(n[1:3]) if len(n) == 4 else int(n[1:3]), int(n[3])): n for n in T7 if n.startswith("a")}
+    amap = {}
+    for n in T7:
+        if n.startswith("a"):
+            i, j = int(n[1:3]), int(n[3:])
+            amap[(i, j)] = n
+    cn = {1: 0.0, 9: 1.0, 10: 1.0}
+    cn.update({int(n[1:]): n for n in T7 if n.startswith("c")})
+    bn = {int(n[1:]): n for n in T7 if re.fullmatch(r"b\d+", n)}
+    btn = {int(n[6:]): n for n in T7 if n.startswith("btilde")}
+    rows, quad, quad_hat, A, b, c = _verner_conditions(T7, 10, cn, amap, bn, btn, 7)
+    assert rows < 1e-13 and quad < 1e-13 and quad_hat < 1e-12
+    # a few tree conditions of order 7
+    assert abs(b @ A @ A @ A @ A @ A @ c - 1 / 5040) < 1e-13
+    assert abs(b @ (c**4 * (A @ c)) - 1 / 14) < 1e-13  # tree [t^4, [t]]: 7 nodes, gamma = 14
+    T9 = parse_tab("VERN9")
+    amap = {(int(n[1:3]), int(n[3:5])): n for n in T9 if re.fullmatch(r"a\d{4}", n)}
+    cn = {1: 0.0, 15: 1.0, 16: 1.0}
+    cn.update({int(n[1:]) + 1: n for n in T9 if re.fullmatch(r"c\d+", n)})
+    bn = {int(n[1:]): n for n in T9 if re.fullmatch(r"b\d+", n)}
+    btn = {int(n[6:]): n for n in T9 if n.startswith("btilde")}
+    rows, quad, quad_hat, A, b, c = _verner_conditions(T9, 16, cn, amap, bn, btn, 9)
+    assert rows < 1e-12 and quad < 1e-12 and quad_hat < 1e-11
+
+
+def test_rodas5p_consistency():
+    """Rodas5P in the W-transformed form: gamma == d1 and 8 solve coefficients per row."""
+    R = parse_tab("RODAS5P")
+    assert R["gamma"] == R["d1"]
+    assert len([n for n in R if n.startswith("C")]) == 28 and len([n for n in R if n.startswith("h")]) == 24
+
+
+# ----------------------------------------------------------------------------- FP64 oracles
+def lorenz_rhs(p):
+    s, r, b = p
+    return lambda t, u: [s * (u[1] - u[0]), u[0] * (r - u[2]) - u[1], u[0] * u[1] - b * u[2]]
+
+
+def test_vern9_matches_dop853(oracle_mod):
+    """FP64 Vern9 at rtol 1e-12 agrees with scipy DOP853 at rtol 1e-13 to <= 1e-9 on
+    non-chaotic Lorenz members."""
+    from scipy.integrate import solve_ivp
+    rng = np.random.default_rng(0)
+    P = np.stack([rng.uniform(1, 10, 8), rng.uniform(0, 20, 8), rng.uniform(0.5, 8 / 3, 8)], 1)
+    u0 = np.tile([1.0, 0.0, 0.0], (8, 1))
+    te = np.linspace(0, 10, 21)
+    v9, _ = oracle_mod.vern9("lorenz", u0, P, 0.0, te)
+    for i in range(8):
+        s = solve_ivp(lorenz_rhs(P[i]), (0, 10), u0[i], method="DOP853", rtol=1e-13, atol=1e-14, t_eval=te)
+        assert np.abs(v9[i] - s.y.T).max() < 1e-9
+
+
+def test_rodas5p_f64_matches_radau(oracle_mod):
+    from scipy.integrate import solve_ivp
+    k = [0.04, 3e7, 1e4]
+
+    def f(t, y):
+        return [-k[0] * y[0] + k[2] * y[1] * y[2], k[0] * y[0] - k[1] * y[1] ** 2 - k[2] * y[1] * y[2], k[1] * y[1] ** 2]
+
+    def J(t, y):
+        return [[-k[0], k[2] * y[2], k[2] * y[1]], [k[0], -2 * k[1] * y[1] - k[2] * y[2], -k[2] * y[1]],
+                [0, 2 * k[1] * y[1], 0]]
+    te = np.logspace(-6, 5, 12)
+    s = solve_ivp(f, (0, 1e5), [1, 0, 0], method="Radau", jac=J, rtol=1e-12, atol=1e-16, t_eval=te)
+    r, _ = oracle_mod.vern9("robertson", np.array([[1.0, 0, 0]]), np.array([k]), 0.0, te, rtol=1e-11, atol=1e-16,
+                            method="rodas5p")
+    assert np.abs(r[0] - s.y.T).max() < 1e-10
+
+
+# ----------------------------------------------------------------------------- known answers / orders
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p"])
+def test_decay_known_answer(oracle_mod, alg):
+    """u' = -u: adaptive solution at the saveat grid vs exp(-t)."""
+    B = 4
+    u0 = np.full((B, 1), 10.0, np.float32)
+    p = np.ones((B, 1), np.float32)
+    sa = np.linspace(0, 1, 11)
+    tol = {"rosenbrock23": 1e-4, "tsit5": 1e-5, "vern7": 1e-5, "rodas5p": 1e-5}[alg]
+    ts, us, rc, _, _ = oracle_mod.solve("decay", alg, u0, p, [0, 1], adaptive=True, dt=0.01, L=11, saveat=sa,
+                                        abstol=1e-8, reltol=1e-8)
+    assert (rc == 1).all()
+    assert np.abs(us[:, :, 0] - 10 * np.exp(-sa)).max() / 10 < tol
+
+
+@pytest.mark.parametrize("alg,dts,lo,hi", [("tsit5", [1.0, 0.5, 0.25], 4.6, 6.2), ("vern7", [2.0, 1.6], 6.3, 9.5),
+                                            ("rosenbrock23", [0.2, 0.1, 0.05], 1.8, 2.3),
+                                            ("rodas5p", [2.0, 1.0], 4.5, 6.5)])
+def test_empirical_order(oracle_mod, alg, dts, lo, hi):
+    """Fixed-step convergence on the harmonic oscillator over (0, 32).  The oracle is FP32,
+    whose round-off floor (~1e-6) hides high orders at small steps, so the step sizes stay
+    in the pre-round-off range and the observed order must fall in [lo, hi]."""
+    u0 = np.array([[1.0, 0.0]], np.float32)
+    p = np.array([[1.0]], np.float32)
+    errs = []
+    for dt in dts:
+        ts, us, _, _, _ = oracle_mod.solve("osc", alg, u0, p, [0, 32], adaptive=False, dt=dt, L=2)
+        t = float(ts[0, 1])  # fixed-step runs end at the reached (overshoot) time
+        errs.append(np.hypot(us[0, 1, 0] - np.cos(t), us[0, 1, 1] + np.sin(t)))
+    obs = [np.log2(errs[i] / errs[i + 1]) / np.log2(dts[i] / dts[i + 1]) for i in range(len(dts) - 1)]
+    assert lo <= np.mean(obs) <= hi, (errs, obs)
+
+
+def test_em_weak_order(oracle_mod):
+    """EM on du = 1.5 u dt + 0.01 u dW: weak error of E[u(1)] ~ O(dt) (order 1 +- 0.15,
+    gpu_sde_convergence.jl:32)."""
+    B = 4000
+    u0 = np.full((B, 1), 0.1, np.float32)
+    p = np.tile(np.array([1.5, 0.01], np.float32), (B, 1))
+    errs = []
+    for k in (3, 4, 5, 6):
+        _, us, _, _, _ = oracle_mod.solve("gbm", "em", u0, p, [0, 1], adaptive=False, dt=2.0 ** -k, L=2, seed=1234)
+        errs.append(abs(us[:, 1, 0].astype(np.float64).mean() - 0.1 * np.exp(1.5)))
+    slope = np.polyfit(np.log2(2.0 ** -np.arange(3, 7)), np.log2(errs), 1)[0]
+    assert abs(slope - 1.0) < 0.15, (errs, slope)
+
+
+@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+def test_reference_regression_tolerances(oracle_mod, alg):
+    """gpu_ode_regression.jl:39-46, 63-72: fixed dt=0.01 within 5e-3 of Vern9 at the final
+    time; adaptive 1e-7 within 1e-3; saveat [2,4] adaptive within 5e-4."""
+    u0 = np.array([[1, 0, 0]], np.float32)
+    p = np.array([[10, 28, 8 / 3]], np.float32)
+    ts, us, _, _, _ = oracle_mod.solve("lorenz", alg, u0, p, [0, 10], adaptive=False, dt=0.01, L=2)
+    v9, _ = oracle_mod.vern9("lorenz", u0, p, 0.0, np.array([float(ts[0, 1])]))
+    assert np.linalg.norm(us[0, 1] - v9[0, 0]) < 5e-3
+    _, us, _, _, _ = oracle_mod.solve("lorenz", alg, u0, p, [0, 10], adaptive=True, dt=0.01, L=2, abstol=1e-7,
+                                      reltol=1e-7)
+    v9, _ = oracle_mod.vern9("lorenz", u0, p, 0.0, np.array([10.0]))
+    assert np.linalg.norm(us[0, 1] - v9[0, 0]) < 1e-3
+    _, us, _, _, _ = oracle_mod.solve("lorenz", alg, u0, p, [0, 10], adaptive=True, dt=0.01, L=2, abstol=1e-7,
+                                      reltol=1e-7, saveat=np.array([2.0, 4.0]))
+    v9, _ = oracle_mod.vern9("lorenz", u0, p, 0.0, np.array([2.0, 4.0]))
+    assert np.linalg.norm(us[0] - v9[0]) < 5e-4
+
+
+def test_stiff_reference_tolerance(oracle_mod):
+    """stiff_ode/gpu_ode_regression.jl:51-59: u' = -u, u0 = 10, fixed dt 0.01 within 5e-3 and
+    adaptive within 6e-3 of the exact solution, for RB23 and Rodas5P."""
+    u0 = np.array([[10.0]], np.float32)
+    p = np.array([[1.0]], np.float32)
+    for alg in ("rosenbrock23", "rodas5p"):
+        _, us, _, _, _ = oracle_mod.solve("decay", alg, u0, p, [0, 10], adaptive=False, dt=0.01, L=2, jac="analytic")
+        assert abs(us[0, 1, 0] - 10 * np.exp(-10.0)) < 5e-3
+        _, us, _, _, _ = oracle_mod.solve("decay", alg, u0, p, [0, 10], adaptive=True, dt=0.01, L=2, jac="analytic",
+                                          abstol=1e-6, reltol=1e-3)
+        assert abs(us[0, 1, 0] - 10 * np.exp(-10.0)) < 6e-3
+
+
+def test_fixed_step_semantics(oracle_mod):
+    """kernels.jl:53-62: with save_everystep=false the second row is the overshoot state at
+    the accumulated Float32 time (100 steps of 0.1f0 end at 10.000002f0)."""
+    u0 = np.array([[1, 0, 0]], np.float32)
+    p = np.array([[10, 28, 8 / 3]], np.float32)
+    ts, us, rc, na, _ = oracle_mod.solve("lorenz", "tsit5", u0, p, [0, 10], adaptive=False, dt=float(np.float32(0.1)),
+                                         L=2)
+    assert na[0] == 100
+    t = np.float32(0)
+    for _ in range(100):
+        t = np.float32(t + np.float32(0.1))
+    assert ts[0, 1] == t and t > np.float32(10)
+
+
+def test_retcodes(oracle_mod):
+    u0 = np.array([[1, 0, 0]] * 3, np.float32)
+    p = np.array([[10, 28, 8 / 3], [np.nan, 28, 8 / 3], [10, 28, 8 / 3]], np.float32)
+    _, _, rc, _, _ = oracle_mod.solve("lorenz", "tsit5", u0, p, [0, 10], adaptive=True, dt=0.1, L=2, maxiters=20)
+    assert rc[0] == 4 and rc[1] in (4, 5)
+
+
+# ----------------------------------------------------------------------------- RNG and portable math
+def test_philox_known_answers(oracle_mod):
+    """Random123's published Philox4x32-10 known-answer vectors."""
+    assert list(oracle_mod.philox([0, 0, 0, 0], [0, 0])) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert list(oracle_mod.philox([0xffffffff] * 4, [0xffffffff] * 2)) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert list(oracle_mod.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0])) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_normals_moments(oracle_mod):
+    z = np.concatenate([oracle_mod.normals4(7, s, t, 0) for s in range(50) for t in range(400)])
+    assert abs(z.mean()) < 0.02 and abs(z.std() - 1) < 0.02
+    assert abs((z**4).mean() - 3) < 0.1
+
+
+def test_portable_pow_accuracy(oracle_mod):
+    rng = np.random.default_rng(1)
+    xs = np.concatenate([10.0 ** rng.uniform(-30, 30, 2000), rng.uniform(0.5, 2, 2000)]).astype(np.float32)
+    for y in (0.14, 0.08, 1 / 35, -1.0 / 9):
+        y32 = np.float32(y)
+        got = np.array([oracle_mod.pm_powf(float(x), float(y32)) for x in xs], np.float64)
+        ref = xs.astype(np.float64) ** np.float64(y32)
+        assert np.abs(got / ref - 1).max() < 4e-6
+    assert oracle_mod.pm_powf(0.0, 0.14) == 0.0
