@@ -114,9 +114,9 @@ def check_kernels(verbose: bool = False) -> list[str]:
         cmd = [NVCC, "-std=c++17", *ARCH, "-Xptxas", "-v", "-c", str(tu), "-o", os.devnull,
                "-I", str(CSRC / "device"), "-I", str(CSRC / "models"),
                f"-DDEGPU_N=3", f"-DDEGPU_P=3", f"-DDEGPU_ALG={alg}", f"-DDEGPU_DRIVER={drv}", f"-DDEGPU_TT={tt}",
-               f"-DDEGPU_PARITY={par}", "-DDEGPU_JAC=0", "-DDEGPU_TGRAD=0", "-DDEGPU_LINSOLVE_REFINE=1"]
-        if par:
-            cmd.append("-fmad=false")
+               f"-DDEGPU_PARITY={par}", "-DDEGPU_JAC=0", "-DDEGPU_TGRAD=0", "-DDEGPU_LINSOLVE_REFINE=1",
+               f"-DDEGPU_TIME_DF={1 if tt == 'double' else 0}"]
+        cmd += ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"] if par else ["-prec-div=false", "-prec-sqrt=false"]
         log = _run(cmd)
         return [f"alg={alg} driver={drv} tt={tt} parity={par}: {ln.strip()}" for ln in log.splitlines() if "registers" in ln]
 

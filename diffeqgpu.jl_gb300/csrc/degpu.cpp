@@ -159,8 +159,8 @@ std::string build_source(const degpu_rhs_s* f, const KernelSpec& k) {
   snprintf(defs, sizeof defs,
            "#define DEGPU_N %d\n#define DEGPU_P %d\n#define DEGPU_TT %s\n#define DEGPU_ALG %d\n"
            "#define DEGPU_DRIVER %d\n#define DEGPU_PARITY %d\n#define DEGPU_JAC %d\n#define DEGPU_TGRAD %d\n"
-           "#define DEGPU_LINSOLVE_REFINE %d\n",
-           f->N, f->P, k.tt ? "double" : "float", k.alg, k.driver, k.parity, k.jac, k.tgrad, k.refine);
+           "#define DEGPU_LINSOLVE_REFINE %d\n#define DEGPU_TIME_DF %d\n",
+           f->N, f->P, k.tt ? "double" : "float", k.alg, k.driver, k.parity, k.jac, k.tgrad, k.refine, k.tt);
   std::string s = defs;
   s += "#include \"degpu_prelude.cuh\"\n#line 1 \"user_rhs.cu\"\n";
   s += f->src;
@@ -200,8 +200,12 @@ int compile_cubin(const std::string& src, bool parity, std::vector<char>& cubin)
   nvrtcProgram prog;
   nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "degpu_tu.cu", (int)hdr_txt.size(), hdr_txt.data(), hdr_names.data());
   if (r != NVRTC_SUCCESS) return fail(DEGPU_E_COMPILE, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
+  // parity: strict IEEE (no contraction, correctly rounded / and sqrt); fast: FMA
+  // contraction and the approximate divide / square root of the SFU
   std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo",
-                                   parity ? "--fmad=false" : "--fmad=true", "--prec-div=true", "--prec-sqrt=true"};
+                                   parity ? "--fmad=false" : "--fmad=true",
+                                   parity ? "--prec-div=true" : "--prec-div=false",
+                                   parity ? "--prec-sqrt=true" : "--prec-sqrt=false"};
   r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
   if (r != NVRTC_SUCCESS) {
     size_t n = 0;

@@ -21,8 +21,55 @@
 
 namespace degpu {
 
-typedef DEGPU_TT Tt;
+typedef DEGPU_TT Tt;  // boundary time type: tspan, saveat and ts are stored as Tt
 constexpr int N = DEGPU_N;
+
+// ------------------------------------------------------------------ time inside the kernels
+// Float32 tspan: time is a float and every operation is the reference's Float32 one.
+// FP64 tspan: time is an unevaluated pair (hi, lo) of floats, hi + lo exactly, advanced by
+// error-free transformations (Knuth's TwoSum, Dekker's Fast2Sum), i.e. ~48-bit time on
+// the FP32 pipes.  GB300 executes FP64 at 1/64 of its FP32 rate, so true FP64 time
+// arithmetic inside the step loop would cost more issue slots than the step itself.
+struct DF { float hi, lo; };
+#if DEGPU_TIME_DF
+struct TP {
+  typedef DF T;
+  static DEGPU_DEV T from(double x) { DF r; r.hi = (float)x; r.lo = (float)(x - (double)r.hi); return r; }
+  static DEGPU_DEV double out(T t) { return (double)t.hi + (double)t.lo; }
+  static DEGPU_DEV T add(T t, float d) {
+    float s = t.hi + d;
+    float bb = s - t.hi;
+    float e = (t.hi - (s - bb)) + (d - bb);
+    e = e + t.lo;
+    DF r;
+    r.hi = s + e;
+    r.lo = e - (r.hi - s);
+    return r;
+  }
+  static DEGPU_DEV float rem(T tf, T t, float dt) { return ((tf.hi - t.hi) + (tf.lo - t.lo)) - dt; }
+  static DEGPU_DEV bool lt(T a, T b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+  static DEGPU_DEV bool le(T a, T b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+  static DEGPU_DEV float stage(T t, float c, float dt) { return t.hi + (t.lo + c * dt); }
+  static DEGPU_DEV float theta(T s, T tp, float dt) { return ((s.hi - tp.hi) + (s.lo - tp.lo)) / dt; }
+  static DEGPU_DEV float em_theta(T s, T t, float dt) { return (((s.hi - t.hi) + (s.lo - t.lo)) + dt) / dt; }
+  static DEGPU_DEV float f32(T t) { return t.hi + t.lo; }
+};
+#else
+struct TP {
+  typedef float T;
+  static DEGPU_DEV T from(float x) { return x; }
+  static DEGPU_DEV float out(T t) { return t; }
+  static DEGPU_DEV T add(T t, float d) { return t + d; }                          // integ.t += dt
+  static DEGPU_DEV float rem(T tf, T t, float dt) { return tf - t - dt; }         // tf - t - dt
+  static DEGPU_DEV bool lt(T a, T b) { return a < b; }
+  static DEGPU_DEV bool le(T a, T b) { return a <= b; }
+  static DEGPU_DEV float stage(T t, float c, float dt) { return t + c * dt; }     // t + c*dt
+  static DEGPU_DEV float theta(T s, T tp, float dt) { return (s - tp) / dt; }     // (savet - tprev)/dt
+  static DEGPU_DEV float em_theta(T s, T t, float dt) { return (s - (t - dt)) / dt; }
+  static DEGPU_DEV float f32(T t) { return t; }
+};
+#endif
+typedef TP::T Time;
 constexpr int NP = DEGPU_P > 0 ? DEGPU_P : 1;
 
 #if DEGPU_ALG == 0
@@ -79,7 +126,7 @@ __constant__ float c_tsit5[TS_COUNT] = {
 #define RP(n) c_rodas5p[RODAS5P_##n]
 
 // ------------------------------------------------------------------ small helpers
-DEGPU_DEV float tstage(Tt t, float c, float dt) { return (float)(t + (Tt)(c * dt)); }
+DEGPU_DEV float tstage(Time t, float c, float dt) { return TP::stage(t, c, dt); }
 
 DEGPU_DEV float ctrl_pow(float x, float y) {
 #if DEGPU_PARITY
@@ -321,7 +368,7 @@ struct Lane {
   float F0[N];
 #endif
   float p[NP];
-  Tt t, tprev, tf, t0;
+  Time t, tprev, tf, t0, next_save;
   float dt, dtnew, qold, abstol, reltol;
   int cur_t, step_idx, nattempt, naccept, nreject, status;
   bool need_begin, fsal;
@@ -331,14 +378,14 @@ struct Lane {
 #if DEGPU_ALG == 0
 DEGPU_DEV void begin_step(Lane& L) {
   // FSAL: k1 = k7 of the previous step unless u was modified (:29-34, :92-97)
-  if (!L.fsal) { rhs(L.k[0], L.uprev, L.p, (float)L.t); L.fsal = true; }
+  if (!L.fsal) { rhs(L.k[0], L.uprev, L.p, TP::f32(L.t)); L.fsal = true; }
   else {
 #pragma unroll
     for (int i = 0; i < N; i++) L.k[0][i] = L.k[6][i];
   }
 }
 template <bool ADAPTIVE>
-DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
+DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
   float tmp[N];
   const float* up = L.uprev;
   float(*k)[N] = L.k;
@@ -356,7 +403,7 @@ DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
   rhs(k[4], tmp, L.p, tstage(t, TS(c4), dt));
 #pragma unroll
   for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (TS(a61) * k[0][i] + TS(a62) * k[1][i] + TS(a63) * k[2][i] + TS(a64) * k[3][i] + TS(a65) * k[4][i]);
-  rhs(k[5], tmp, L.p, (float)(t + (Tt)dt));
+  rhs(k[5], tmp, L.p, tstage(t, 1.0f, dt));
 #pragma unroll
   for (int i = 0; i < N; i++) {
     if (ADAPTIVE)  // :114
@@ -364,7 +411,7 @@ DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
     else  // :47-48
       u[i] = up[i] + dt * ((TS(a71) * k[0][i] + TS(a72) * k[1][i] + TS(a73) * k[2][i] + TS(a74) * k[3][i]) + TS(a75) * k[4][i] + TS(a76) * k[5][i]);
   }
-  rhs(k[6], u, L.p, (float)(t + (Tt)dt));
+  rhs(k[6], u, L.p, tstage(t, 1.0f, dt));
   if (ADAPTIVE) {
 #pragma unroll
     for (int i = 0; i < N; i++)
@@ -390,10 +437,10 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 #if DEGPU_ALG == 1
 DEGPU_DEV void begin_step(Lane& L) {
   // not FSAL: k1 = f(uprev, p, t) every step (:30, :117; one evaluation per step suffices)
-  rhs(L.k[0], L.uprev, L.p, (float)L.t);
+  rhs(L.k[0], L.uprev, L.p, TP::f32(L.t));
 }
 template <bool ADAPTIVE>
-DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
+DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
   float tmp[N];
   const float* up = L.uprev;
   float(*k)[N] = L.k;
@@ -425,8 +472,8 @@ DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
     tmp[i] = up[i] + dt * (V7(a091) * k[0][i] + V7(a093) * k[2][i] + V7(a094) * k[3][i] + V7(a095) * k[4][i] + V7(a096) * k[5][i] + V7(a097) * k[6][i] + V7(a098) * k[7][i]);
     g10[i] = up[i] + dt * (V7(a101) * k[0][i] + V7(a103) * k[2][i] + V7(a104) * k[3][i] + V7(a105) * k[4][i] + V7(a106) * k[5][i] + V7(a107) * k[6][i]);
   }
-  rhs(k[8], tmp, L.p, (float)(t + (Tt)dt));
-  rhs(k[9], g10, L.p, (float)(t + (Tt)dt));
+  rhs(k[8], tmp, L.p, tstage(t, 1.0f, dt));
+  rhs(k[9], g10, L.p, tstage(t, 1.0f, dt));
 #pragma unroll
   for (int i = 0; i < N; i++)
     u[i] = up[i] + dt * (V7(b1) * k[0][i] + V7(b4) * k[3][i] + V7(b5) * k[4][i] + V7(b6) * k[5][i] + V7(b7) * k[6][i] + V7(b8) * k[7][i] + V7(b9) * k[8][i]);
@@ -459,7 +506,7 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
   const float* up = L.uprev;
   const float(*k)[N] = L.k;
   float k11[N], k12[N], k13[N], k14[N], k15[N], k16[N], tmp[N];
-  Tt tp = L.tprev;
+  Time tp = L.tprev;
 #pragma unroll
   for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V7X(a1101) * k[0][i] + V7X(a1104) * k[3][i] + V7X(a1105) * k[4][i] + V7X(a1106) * k[5][i] + V7X(a1107) * k[6][i] + V7X(a1108) * k[7][i] + V7X(a1109) * k[8][i]);
   rhs(k11, tmp, L.p, tstage(tp, V7X(c11), dt));
@@ -492,13 +539,13 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 #if DEGPU_ALG == 2
 DEGPU_DEV void begin_step(Lane& L) {
   // J, dT and F0 = f(uprev, t) depend only on (uprev, t): once per step (:38-49, :114-124)
-  float tf_ = (float)L.t;
+  float tf_ = TP::f32(L.t);
   jacobian(L.J, L.uprev, L.p, tf_);
   tgrad(L.dT, L.uprev, L.p, tf_);
   rhs(L.F0, L.uprev, L.p, tf_);
 }
 template <bool ADAPTIVE>
-DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
+DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
   const float d = 1.0f / (2.0f + sqrtf(2.0f));
   float gam = dt * d, dto2 = dt / 2.0f, dto6 = dt / 6.0f;
   LinSys S;
@@ -517,7 +564,7 @@ DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
   S.solve(rhsv, k1);
 #pragma unroll
   for (int i = 0; i < N; i++) tmp[i] = L.uprev[i] + dto2 * k1[i];
-  rhs(F1, tmp, L.p, (float)(t + (Tt)dto2));
+  rhs(F1, tmp, L.p, tstage(t, 1.0f, dto2));
 #pragma unroll
   for (int i = 0; i < N; i++) rhsv[i] = F1[i] - k1[i];
   S.solve(rhsv, k2);
@@ -526,7 +573,7 @@ DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* u, float* err) {
   if (ADAPTIVE) {
     const float e32 = 6.0f + sqrtf(2.0f);
     float F2[N], k3[N];
-    rhs(F2, u, L.p, (float)(t + (Tt)dt));
+    rhs(F2, u, L.p, tstage(t, 1.0f, dt));
 #pragma unroll
     for (int i = 0; i < N; i++) rhsv[i] = F2[i] - e32 * (k2[i] - F1[i]) - 2.0f * (k1[i] - L.F0[i]) + dt * L.dT[i];
     S.solve(rhsv, k3);
@@ -547,12 +594,12 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 // ------------------------------------------------------------------ Rodas5P (gpu_rodas5P_perform_step.jl)
 #if DEGPU_ALG == 3
 DEGPU_DEV void begin_step(Lane& L) {
-  float tf_ = (float)L.t;  // J, dT once per step, outside the reject loop (:182-186)
+  float tf_ = TP::f32(L.t);  // J, dT once per step, outside the reject loop (:182-186)
   jacobian(L.J, L.uprev, L.p, tf_);
   tgrad(L.dT, L.uprev, L.p, tf_);
 }
 template <bool ADAPTIVE>
-DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* uout, float* err) {
+DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* uout, float* err) {
   const float* up = L.uprev;
   float dtC21 = RP(C21) / dt, dtC31 = RP(C31) / dt, dtC32 = RP(C32) / dt, dtC41 = RP(C41) / dt, dtC42 = RP(C42) / dt, dtC43 = RP(C43) / dt;
   float dtC51 = RP(C51) / dt, dtC52 = RP(C52) / dt, dtC53 = RP(C53) / dt, dtC54 = RP(C54) / dt;
@@ -577,7 +624,7 @@ DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* uout, float* err) {
     _Pragma("unroll") for (int i = 0; i < N; i++) lt[i] = -lt[i]; \
     S.solve(lt, K);                               \
   }
-  rhs(du, up, L.p, (float)t);
+  rhs(du, up, L.p, TP::f32(t));
 #pragma unroll
   for (int i = 0; i < N; i++) lt[i] = du[i] + dtd1 * L.dT[i];
   SOLVE(k1);
@@ -607,19 +654,19 @@ DEGPU_DEV void attempt(Lane& L, Tt t, float dt, float* uout, float* err) {
   SOLVE(k5);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + RP(a61) * k1[i] + RP(a62) * k2[i] + RP(a63) * k3[i] + RP(a64) * k4[i] + RP(a65) * k5[i];
-  rhs(du, u, L.p, (float)(t + (Tt)dt));
+  rhs(du, u, L.p, tstage(t, 1.0f, dt));
 #pragma unroll
   for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC63 * k3[i] + dtC64 * k4[i] + dtC65 * k5[i]);
   SOLVE(k6);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = u[i] + k6[i];
-  rhs(du, u, L.p, (float)(t + (Tt)dt));
+  rhs(du, u, L.p, tstage(t, 1.0f, dt));
 #pragma unroll
   for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC71 * k1[i] + dtC72 * k2[i] + dtC73 * k3[i] + dtC74 * k4[i] + dtC75 * k5[i] + dtC76 * k6[i]);
   SOLVE(k7);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = u[i] + k7[i];
-  rhs(du, u, L.p, (float)(t + (Tt)dt));
+  rhs(du, u, L.p, tstage(t, 1.0f, dt));
 #pragma unroll
   for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC81 * k1[i] + dtC82 * k2[i] + dtC83 * k3[i] + dtC84 * k4[i] + dtC85 * k5[i] + dtC86 * k6[i] + dtC87 * k7[i]);
   SOLVE(k8);
@@ -663,8 +710,9 @@ struct Io {
 DEGPU_DEV void lane_init(Lane& L, const Io& io, long long i) {
   const degpu_kparams& P = io.P;
   const Tt* tsp = (const Tt*)P.tspan + 2 * i;
-  L.t0 = tsp[0];
-  L.tf = tsp[1];
+  const Tt t0_in = tsp[0];
+  L.t0 = TP::from(t0_in);
+  L.tf = TP::from(tsp[1]);
   L.t = L.t0;
   L.tprev = L.t0;
 #pragma unroll
@@ -691,7 +739,9 @@ DEGPU_DEV void lane_init(Lane& L, const Io& io, long long i) {
   L.need_begin = true;
   L.fsal = false;
   if (P.nsaveat) {
-    if (L.t0 == io.saveat(i, 0)) { L.cur_t = 1; io.store_u(i, 0, L.u); }
+    const Tt s0 = io.saveat(i, 0);
+    if (t0_in == s0) { L.cur_t = 1; io.store_u(i, 0, L.u); }
+    L.next_save = TP::from(L.cur_t < P.nsaveat ? io.saveat(i, L.cur_t) : s0);
   } else {
     io.store_u(i, 0, L.u);
   }
@@ -701,26 +751,26 @@ DEGPU_DEV void lane_init(Lane& L, const Io& io, long long i) {
 DEGPU_DEV void save_values(Lane& L, const Io& io, long long i, bool save_everystep) {
   const degpu_kparams& P = io.P;
   if (P.nsaveat) {
-    while (L.cur_t < P.nsaveat) {
-      Tt savet = io.saveat(i, L.cur_t);
-      if (!(savet <= L.t)) break;
-      float th = (float)((savet - L.tprev) / (Tt)L.dt);
+    // the next save time is cached in registers: one compare per step, no global load
+    while (L.cur_t < P.nsaveat && TP::le(L.next_save, L.t)) {
+      float th = TP::theta(L.next_save, L.tprev, L.dt);
       if (L.cur_t < P.L) {
         float v[N];
         interp(L, th, L.dt, v);
         io.store_u(i, L.cur_t, v);
       }
       L.cur_t++;
+      if (L.cur_t < P.nsaveat) L.next_save = TP::from(io.saveat(i, L.cur_t));
     }
   } else if (save_everystep) {
-    if (L.step_idx < P.L) { io.store_u(i, L.step_idx, L.u); io.ts(i)[L.step_idx] = L.t; }
+    if (L.step_idx < P.L) { io.store_u(i, L.step_idx, L.u); io.ts(i)[L.step_idx] = TP::out(L.t); }
     L.step_idx++;
   }
 }
 
 // PI controller, integrator_utils.jl:1-11 constants, decision as in
 // gpu_tsit5_perform_step.jl:124-170.  Returns true on accept.
-DEGPU_DEV bool controller(Lane& L, float EEst, float& dt, Tt t) {
+DEGPU_DEV bool controller(Lane& L, float EEst, float& dt, Time t) {
   const float beta1 = (float)(7.0 / (10.0 * ORDER)), beta2 = (float)(2.0 / (5.0 * ORDER));
   const float qmax = 10.0f, qmin = (float)(1.0 / 5.0), gamma = (float)(9.0 / 10.0), qoldinit = (float)1.0e-4;
   float q11 = 0.0f, q;
@@ -733,11 +783,11 @@ DEGPU_DEV bool controller(Lane& L, float EEst, float& dt, Tt t) {
   q = jl_max(1.0f / qmax, jl_min(1.0f / qmin, q / gamma));
   L.qold = jl_max(EEst, qoldinit);
   float dtnew = dt / q;
-  Tt rem = L.tf - t - (Tt)dt;
-  L.dtnew = (float)(Tt)jl_mind((double)fabsf(dtnew), fabs((double)rem));
+  float rem = TP::rem(L.tf, t, dt);
+  L.dtnew = jl_min(fabsf(dtnew), fabsf(rem));
   L.dt = dt;
   L.tprev = t;
-  L.t = (rem < (Tt)1.0e-14) ? L.tf : t + (Tt)dt;  // end snap (:155-156)
+  L.t = (rem < 1.0e-14f) ? L.tf : TP::add(t, dt);  // end snap (:155-156)
   return true;
 }
 
@@ -751,7 +801,7 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, long long i) {
     begin_step(L);
     L.need_begin = false;
   }
-  Tt t = L.t;
+  Time t = L.t;
   float unew[N], err[N];
   if (ADAPTIVE) {
     float dt = L.dtnew;
@@ -768,7 +818,7 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, long long i) {
     if (++L.nattempt > P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
     float dt = L.dt;
     L.tprev = t;
-    L.t = t + (Tt)dt;
+    L.t = TP::add(t, dt);
     attempt<false>(L, t, dt, unew, err);
   }
 #pragma unroll
@@ -776,26 +826,27 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, long long i) {
   L.naccept++;
   L.need_begin = true;
   save_values(L, io, i, !ADAPTIVE && P.save_everystep);
-  return !(L.t < L.tf);
+  return !TP::lt(L.t, L.tf);
 }
 
 // end of the driver loop (kernels.jl:53-62, 133-142) and outputs
 DEGPU_DEV void lane_finish(Lane& L, const Io& io, long long i) {
   const degpu_kparams& P = io.P;
   Tt* ts = io.ts(i);
+  const Tt t0_in = ((const Tt*)P.tspan)[2 * i];  // fill! ts with tspan[1] (lowerlevel_solve.jl:82)
   if (P.nsaveat) {
-    for (int l = 0; l < P.L; l++) ts[l] = (l < L.cur_t) ? io.saveat(i, l) : L.t0;
+    for (int l = 0; l < P.L; l++) ts[l] = (l < L.cur_t) ? io.saveat(i, l) : t0_in;
   } else {
     int first_unset = P.save_everystep ? (L.step_idx < P.L ? L.step_idx : P.L) : 1;
-    ts[0] = L.t0;
-    for (int l = first_unset; l < P.L; l++) ts[l] = L.t0;
-    if (L.t > L.tf && P.save_everystep) {
+    ts[0] = t0_in;
+    for (int l = first_unset; l < P.L; l++) ts[l] = t0_in;
+    if (TP::lt(L.tf, L.t) && P.save_everystep) {
       float v[N];
-      interp(L, (float)((L.tf - L.tprev) / (Tt)L.dt), L.dt, v);
+      interp(L, TP::theta(L.tf, L.tprev, L.dt), L.dt, v);
       io.store_u(i, P.L - 1, v);
-      ts[P.L - 1] = L.tf;
+      ts[P.L - 1] = ((const Tt*)P.tspan)[2 * i + 1];
     }
-    if (!P.save_everystep) { io.store_u(i, 1, L.u); ts[1] = L.t; }
+    if (!P.save_everystep) { io.store_u(i, 1, L.u); ts[1] = TP::out(L.t); }
   }
   if (L.status == DEGPU_RET_DEFAULT) {
     bool fin = true;
@@ -821,7 +872,7 @@ extern "C" __global__ void __launch_bounds__(256) degpu_solve_kernel(const degpu
   Io io{P};
   Lane L;
   lane_init(L, io, i);
-  bool done = !(L.t < L.tf);
+  bool done = !TP::lt(L.t, L.tf);
   while (!done) done = advance<DEGPU_DRIVER == 1>(L, io, i);
   lane_finish(L, io, i);
 }
@@ -861,7 +912,7 @@ extern "C" __global__ void __launch_bounds__(256) degpu_persistent_kernel(const 
       if (my < 0 && q_next + rank < q_end) {
         my = q_next + rank;
         lane_init(L, io, my);
-        if (!(L.t < L.tf)) { lane_finish(L, io, my); my = -1; }
+        if (!TP::lt(L.t, L.tf)) { lane_finish(L, io, my); my = -1; }
       }
       q_next = min(q_next + (long long)__popc(idle), q_end);
     }
@@ -920,9 +971,9 @@ extern "C" __global__ void __launch_bounds__(256) degpu_em_kernel(const degpu_kp
   if (i >= P.B) return;
   const int L = P.L;
   const Tt* tsp = (const Tt*)P.tspan + 2 * i;
-  Tt t0 = tsp[0], tf = tsp[1];
-  Tt dtT = (Tt)P.dt;
-  float dt = (float)dtT;
+  const Tt t0_in = tsp[0], tf_in = tsp[1];
+  const Tt dtT = (Tt)P.dt;
+  const float dt = (float)dtT;
   Tt* ts = (Tt*)P.ts + i * L;
   float* us = P.us + i * (long long)L * N;
   const Tt* sa = P.nsaveat ? (const Tt*)P.saveat + (P.saveat_per_traj ? i * P.nsaveat : 0) : nullptr;
@@ -933,41 +984,45 @@ extern "C" __global__ void __launch_bounds__(256) degpu_em_kernel(const degpu_kp
   float u[N], up[N], f[N], g[N], z[(N + 3) / 4 * 4];
 #pragma unroll
   for (int c = 0; c < N; c++) u[c] = P.u0[i * N + c];
-  for (int l = 0; l < L; l++) ts[l] = t0;
+  for (int l = 0; l < L; l++) ts[l] = t0_in;
+  Time next_save = TP::from(t0_in);
   if (sa) {
-    if (t0 == sa[0]) { cur_t = 1; for (int c = 0; c < N; c++) us[c] = u[c]; }
+    if (t0_in == sa[0]) { cur_t = 1; for (int c = 0; c < N; c++) us[c] = u[c]; }
+    if (cur_t < P.nsaveat) next_save = TP::from(sa[cur_t]);
   } else {
     for (int c = 0; c < N; c++) us[c] = u[c];
   }
   float sqdt = sqrtf(dt);
-  Tt t = t0;
-  Tt span = tf - t0;
-  Tt ratio = (span < 0 ? -span : span) / (dtT < 0 ? -dtT : dtT);
+  Time t = TP::from(t0_in);
+  // n = floor(Int, abs(tf - t0) / abs(dt)) + 1 (:44), in the boundary time type
+  const Tt span = tf_in - t0_in;
+  const Tt dtb = (Tt)dt;
+  const Tt ratio = (span < 0 ? -span : span) / (dtb < 0 ? -dtb : dtb);
   long long n = (long long)floor((double)ratio) + 1;
   if (n - 1 > P.maxiters) n = P.maxiters + 1;
   const uint32_t gi = (uint32_t)(P.traj_offset + i);
   for (long long j = 2; j <= n; j++) {
 #pragma unroll
     for (int c = 0; c < N; c++) up[c] = u[c];
-    degpu_f<float>(f, up, p, (float)t);
-    degpu_g<float>(g, up, p, (float)t);
+    degpu_f<float>(f, up, p, TP::f32(t));
+    degpu_g<float>(g, up, p, TP::f32(t));
 #pragma unroll
     for (int b = 0; b < (N + 3) / 4; b++) normals4(P.seed, (uint32_t)(j - 2), gi, (uint32_t)b, z + 4 * b);
 #pragma unroll
     for (int c = 0; c < N; c++) u[c] = up[c] + f[c] * dt + (sqdt * g[c]) * z[c];
-    t = t + (Tt)dt;
+    t = TP::add(t, dt);
     if (!sa && P.save_everystep) {
-      if (j - 1 < L) { for (int c = 0; c < N; c++) us[(j - 1) * N + c] = u[c]; ts[j - 1] = t; }
+      if (j - 1 < L) { for (int c = 0; c < N; c++) us[(j - 1) * N + c] = u[c]; ts[j - 1] = TP::out(t); }
     } else if (sa) {
-      while (cur_t < P.nsaveat && sa[cur_t] <= t) {
-        Tt savet = sa[cur_t];
-        float th = (float)((savet - (t - (Tt)dt)) / (Tt)dt);
-        if (cur_t < L) { for (int c = 0; c < N; c++) us[cur_t * N + c] = up[c] + (u[c] - up[c]) * th; ts[cur_t] = savet; }
+      while (cur_t < P.nsaveat && TP::le(next_save, t)) {
+        float th = TP::em_theta(next_save, t, dt);
+        if (cur_t < L) { for (int c = 0; c < N; c++) us[cur_t * N + c] = up[c] + (u[c] - up[c]) * th; ts[cur_t] = sa[cur_t]; }
         cur_t++;
+        if (cur_t < P.nsaveat) next_save = TP::from(sa[cur_t]);
       }
     }
   }
-  if (!sa && !P.save_everystep) { for (int c = 0; c < N; c++) us[N + c] = u[c]; ts[1] = t; }
+  if (!sa && !P.save_everystep) { for (int c = 0; c < N; c++) us[N + c] = u[c]; ts[1] = TP::out(t); }
   if (P.retcode) {
     bool fin = true;
     for (int c = 0; c < N; c++) fin = fin && isfinite(u[c]);

@@ -175,6 +175,33 @@ int degpu_rhs_check(const degpu_rhs* f, const degpu_options* opt, int adaptive, 
 int degpu_kernel_info(const degpu_rhs* f, const degpu_options* opt, int adaptive, int* regs, int* local_bytes,
                       int* max_threads);
 
+/* ---- learned step control (no counterpart in the reference) ----
+ * A BF16 MLP  x -> 64 SiLU -> 64 SiLU -> 2  predicting, per trajectory, log(initial dt) and
+ * log(tolerance scale) from x = (u0, p, log10 reltol) (n_in <= 16).  Its outputs feed
+ * degpu_options.dt0 / .tolscale; the embedded error estimate still accepts or rejects
+ * every step.  Parameters are one packed FP32 vector (W1 [64][n_in], b1 [64], W2 [64][64],
+ * b2 [64], W3 [2][64], b3 [2]); inputs are standardised with (mean, std) inside. */
+#define DEGPU_MLP_HIDDEN 64
+#define DEGPU_MLP_OUT 2
+typedef struct degpu_mlp_s degpu_mlp;
+int degpu_mlp_create(int n_in, unsigned long long seed, degpu_mlp** out);
+void degpu_mlp_destroy(degpu_mlp* m);
+int degpu_mlp_param_count(const degpu_mlp* m);
+/* host arrays; any may be NULL */
+int degpu_mlp_set_params(degpu_mlp* m, const float* host_params, const float* host_mean, const float* host_std);
+int degpu_mlp_get_params(const degpu_mlp* m, float* host_params, float* host_grads, float* host_mean, float* host_std);
+/* Tensor-core inference (mma.sync m16n8k16 bf16, fp32 accumulate) over device x [B][n_in]:
+ * y [B][2] raw outputs (optional), dt0 = clamp(exp(y0), dt_lo, dt_hi), tolscale =
+ * clamp(exp(y1), s_lo, s_hi) (each optional). */
+int degpu_mlp_infer(const degpu_mlp* m, const float* x, long long B, float* y, float* dt0, float* tolscale,
+                    float dt_lo, float dt_hi, float s_lo, float s_hi, void* stream);
+/* Gradient of the weighted mean squared error over a device batch (target, weight [B][2];
+ * weight may be NULL) into the model's gradient buffer; *loss (device scalar, optional). */
+int degpu_mlp_grad(degpu_mlp* m, const float* x, const float* target, const float* weight, long long B, float* loss,
+                   void* stream);
+/* One Adam step (bias-corrected) with decoupled-into-gradient weight decay. */
+int degpu_mlp_adam_step(degpu_mlp* m, float lr, float beta1, float beta2, float eps, float weight_decay, void* stream);
+
 /* ---- measurement utilities (no counterpart in the reference) ---- */
 /* Sustained FP32 FMA throughput of the current device in TFLOP/s (8 independent FMA
  * chains per thread over a grid that fills every SM); the roofline denominator that

@@ -32,8 +32,9 @@
  *   - interpolants (`@muladd` in the reference) are evaluated without FMA;
  *   - `error("dt<dtmin")` becomes retcode DtLessThanMin, and an attempt cap (maxiters)
  *     ends runaway trajectories with retcode MaxIters instead of looping forever;
- *   - time may be FP64 (Tt = double) with FP32 state.  With Tt = float every operation
- *     is the reference's Float32 operation.
+ *   - with an FP64 tspan, time is held as an unevaluated float pair (hi, lo) advanced by
+ *     error-free TwoSum/Fast2Sum (the kernels' FP64-time mode, ~48-bit time on FP32
+ *     pipes); with a Float32 tspan every time operation is the reference's Float32 one.
  * Parity status: bit-faithful restatement for the fixed-step explicit RK path (only
  * +,-,* in a fixed order); adaptive paths pinned by the FP64 Vern9 solution and the
  * reference's own test tolerances -- the reference (Julia) cannot run in this build.
@@ -202,6 +203,44 @@ static inline float jl_min(float x, float y) { if (x != x) return x; if (y != y)
 static inline float jl_max(float x, float y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
 static inline double jl_mind(double x, double y) { if (x != x) return x; if (y != y) return y; return y < x ? y : x; }
 
+/* ------------------------------------------------------------------ time arithmetic
+ * float: the reference's Float32 time.  DF: hi + lo exactly, TwoSum (Knuth) + Fast2Sum
+ * (Dekker) accumulation -- the same operations, in the same order, as the kernels. */
+struct DF { float hi, lo; };
+template <class Tt> struct TOut;
+template <> struct TOut<float> { typedef float T; };
+template <> struct TOut<DF> { typedef double T; };
+template <class Tt> static inline Tt t_from(double x);
+template <> inline float t_from<float>(double x) { return (float)x; }
+template <> inline DF t_from<DF>(double x) { DF r; r.hi = (float)x; r.lo = (float)(x - (double)r.hi); return r; }
+static inline float t_out(float t) { return t; }
+static inline double t_out(DF t) { return (double)t.hi + (double)t.lo; }
+static inline float t_add(float t, float d) { return t + d; }
+static inline DF t_add(DF t, float d) {
+  float s = t.hi + d;
+  float bb = s - t.hi;
+  float e = (t.hi - (s - bb)) + (d - bb);
+  e = e + t.lo;
+  DF r;
+  r.hi = s + e;
+  r.lo = e - (r.hi - s);
+  return r;
+}
+static inline float t_rem(float tf, float t, float dt) { return tf - t - dt; }
+static inline float t_rem(DF tf, DF t, float dt) { return ((tf.hi - t.hi) + (tf.lo - t.lo)) - dt; }
+static inline bool t_lt(float a, float b) { return a < b; }
+static inline bool t_lt(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+static inline bool t_le(float a, float b) { return a <= b; }
+static inline bool t_le(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+static inline float t_stage(float t, float c, float dt) { return t + c * dt; }
+static inline float t_stage(DF t, float c, float dt) { return t.hi + (t.lo + c * dt); }
+static inline float t_theta(float s, float tp, float dt) { return (s - tp) / dt; }
+static inline float t_theta(DF s, DF tp, float dt) { return ((s.hi - tp.hi) + (s.lo - tp.lo)) / dt; }
+static inline float t_em_theta(float s, float t, float dt) { return (s - (t - dt)) / dt; }
+static inline float t_em_theta(DF s, DF t, float dt) { return (((s.hi - t.hi) + (s.lo - t.lo)) + dt) / dt; }
+static inline float t_f32(float t) { return t; }
+static inline float t_f32(DF t) { return t.hi + t.lo; }
+
 /* DiffEqBase.ODE_DEFAULT_NORM for a static vector: sqrt(sum(abs2, u) / length(u)) */
 static inline float ode_norm(const float* x, int N) {
   float s = x[0] * x[0];
@@ -296,7 +335,7 @@ template <class Tt> struct Integ {
 };
 
 /* time argument handed to f: `t + c*dt` in Tt, passed to the FP32 right-hand side */
-template <class Tt> static inline float tstage(Tt t, float c, float dt) { return (float)(t + (Tt)(c * dt)); }
+template <class Tt> static inline float tstage(Tt t, float c, float dt) { return t_stage(t, c, dt); }
 
 /* ------------------------------------------------------------------ Tsit5 */
 /* stage block shared by gpu_tsit5_perform_step.jl:36-49 (fixed) and :104-115 (adaptive).
@@ -316,14 +355,14 @@ static void tsit5_stages(int m, Integ<Tt>& ig, const float* p, Tt t, float dt, c
   for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (T.a51 * k1[i] + T.a52 * k2[i] + T.a53 * k3[i] + T.a54 * k4[i]);
   model_f<float>(m, k5, tmp, p, tstage(t, T.c4, dt));
   for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (T.a61 * k1[i] + T.a62 * k2[i] + T.a63 * k3[i] + T.a64 * k4[i] + T.a65 * k5[i]);
-  model_f<float>(m, k6, tmp, p, (float)(t + (Tt)dt));
+  model_f<float>(m, k6, tmp, p, t_stage(t, 1.0f, dt));
   for (int i = 0; i < N; i++) {
     if (fixed_grouping)
       u[i] = up[i] + dt * ((T.a71 * k1[i] + T.a72 * k2[i] + T.a73 * k3[i] + T.a74 * k4[i]) + T.a75 * k5[i] + T.a76 * k6[i]);
     else
       u[i] = up[i] + dt * (T.a71 * k1[i] + T.a72 * k2[i] + T.a73 * k3[i] + T.a74 * k4[i] + T.a75 * k5[i] + T.a76 * k6[i]);
   }
-  model_f<float>(m, k7, u, p, (float)(t + (Tt)dt));
+  model_f<float>(m, k7, u, p, t_stage(t, 1.0f, dt));
   for (int i = 0; i < N; i++) {
     k[0][i] = k1[i]; k[1][i] = k2[i]; k[2][i] = k3[i]; k[3][i] = k4[i];
     k[4][i] = k5[i]; k[5][i] = k6[i]; k[6][i] = k7[i];
@@ -350,7 +389,7 @@ static void vern7_stages(int m, Integ<Tt>& ig, const float* p, Tt t, float dt, f
   float tmp[MAXN];
   float* k1 = k[0]; float* k2 = k[1]; float* k3 = k[2]; float* k4 = k[3]; float* k5 = k[4];
   float* k6 = k[5]; float* k7 = k[6]; float* k8 = k[7]; float* k9 = k[8]; float* k10 = k[9];
-  model_f<float>(m, k1, up, p, (float)t);
+  model_f<float>(m, k1, up, p, t_f32(t));
   float a = dt * V7C(a021);
   for (int i = 0; i < N; i++) tmp[i] = up[i] + a * k1[i];
   model_f<float>(m, k2, tmp, p, tstage(t, V7C(c2), dt));
@@ -371,8 +410,8 @@ static void vern7_stages(int m, Integ<Tt>& ig, const float* p, Tt t, float dt, f
     g9[i] = up[i] + dt * (V7C(a091) * k1[i] + V7C(a093) * k3[i] + V7C(a094) * k4[i] + V7C(a095) * k5[i] + V7C(a096) * k6[i] + V7C(a097) * k7[i] + V7C(a098) * k8[i]);
     g10[i] = up[i] + dt * (V7C(a101) * k1[i] + V7C(a103) * k3[i] + V7C(a104) * k4[i] + V7C(a105) * k5[i] + V7C(a106) * k6[i] + V7C(a107) * k7[i]);
   }
-  model_f<float>(m, k9, g9, p, (float)(t + (Tt)dt));
-  model_f<float>(m, k10, g10, p, (float)(t + (Tt)dt));
+  model_f<float>(m, k9, g9, p, t_stage(t, 1.0f, dt));
+  model_f<float>(m, k10, g10, p, t_stage(t, 1.0f, dt));
   for (int i = 0; i < N; i++)
     u[i] = up[i] + dt * (V7C(b1) * k1[i] + V7C(b4) * k4[i] + V7C(b5) * k5[i] + V7C(b6) * k6[i] + V7C(b7) * k7[i] + V7C(b8) * k8[i] + V7C(b9) * k9[i]);
 }
@@ -497,12 +536,12 @@ static int controller(Integ<Tt>& ig, const Ctrl& C, float EEst, float& dt, Tt t)
   q = jl_max(1.0f / C.qmax, jl_min(1.0f / C.qmin, q / C.gamma));
   ig.qold = jl_max(EEst, C.qoldinit);
   float dtnew = dt / q;
-  Tt rem = ig.tf - t - (Tt)dt;
-  ig.dtnew = (float)(Tt)jl_mind((double)fabsf(dtnew), fabs((double)rem));
+  float rem = t_rem(ig.tf, t, dt);
+  ig.dtnew = jl_min(fabsf(dtnew), fabsf(rem));
   ig.dt = dt;
   ig.tprev = t;
-  if (rem < (Tt)1.0e-14) ig.t = ig.tf;
-  else ig.t = t + (Tt)dt;
+  if (rem < 1.0e-14f) ig.t = ig.tf;
+  else ig.t = t_add(t, dt);
   return 1;
 }
 
@@ -519,7 +558,7 @@ static void rb23_attempt(int m, int jacmode, Integ<Tt>& ig, const float* p, Tt t
   int N = ig.N;
   const float d = 1.0f / (2.0f + sqrtf(2.0f));
   float J[MAXN * MAXN], dT[MAXN], W[MAXN * MAXN], F0[MAXN], F1[MAXN], F2[MAXN], rhs[MAXN], tmp[MAXN], k1[MAXN], k2[MAXN], k3[MAXN];
-  float tf_ = (float)t;
+  float tf_ = t_f32(t);
   float gam = dt * d, dto2 = dt / 2.0f, dto6 = dt / 6.0f;
   compute_J(m, jacmode, N, J, ig.uprev, p, tf_);
   compute_tgrad(m, jacmode, N, dT, ig.uprev, p, tf_);
@@ -528,7 +567,7 @@ static void rb23_attempt(int m, int jacmode, Integ<Tt>& ig, const float* p, Tt t
   for (int i = 0; i < N; i++) rhs[i] = F0[i] + gam * dT[i];
   linear_solve(N, W, rhs, k1);
   for (int i = 0; i < N; i++) tmp[i] = ig.uprev[i] + dto2 * k1[i];
-  model_f<float>(m, F1, tmp, p, (float)(t + (Tt)dto2));
+  model_f<float>(m, F1, tmp, p, t_stage(t, 1.0f, dto2));
   for (int i = 0; i < N; i++) rhs[i] = F1[i] - k1[i];
   linear_solve(N, W, rhs, k2);
   for (int i = 0; i < N; i++) k2[i] = k2[i] + k1[i];
@@ -536,7 +575,7 @@ static void rb23_attempt(int m, int jacmode, Integ<Tt>& ig, const float* p, Tt t
   for (int i = 0; i < N; i++) { k1o[i] = k1[i]; k2o[i] = k2[i]; }
   if (!adaptive) return;
   const float e32 = 6.0f + sqrtf(2.0f);
-  model_f<float>(m, F2, u, p, (float)(t + (Tt)dt));
+  model_f<float>(m, F2, u, p, t_stage(t, 1.0f, dt));
   for (int i = 0; i < N; i++) rhs[i] = F2[i] - e32 * (k2[i] - F1[i]) - 2.0f * (k1[i] - F0[i]) + dt * dT[i];
   linear_solve(N, W, rhs, k3);
   for (int i = 0; i < N; i++) err[i] = dto6 * (k1[i] - 2.0f * k2[i] + k3[i]);
@@ -559,7 +598,7 @@ static void rodas5p_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt
   for (int j = 0; j < N; j++) for (int i = 0; i < N; i++) W[i + N * j] = J[i + N * j] - (i == j ? 1.0f : 0.0f) * inv_dtg;
   float du[MAXN], u[MAXN], lt[MAXN], neg[MAXN];
   float k1[MAXN], k2[MAXN], k3[MAXN], k4[MAXN], k5[MAXN], k6[MAXN], k7[MAXN], k8[MAXN];
-  float tf_ = (float)t;
+  float tf_ = t_f32(t);
 #define SOLVE(K) { for (int i = 0; i < N; i++) neg[i] = -lt[i]; linear_solve(N, W, neg, K); }
   model_f<float>(m, du, up, p, tf_);
   for (int i = 0; i < N; i++) lt[i] = du[i] + dtd1 * dT[i];
@@ -581,15 +620,15 @@ static void rodas5p_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt
   for (int i = 0; i < N; i++) lt[i] = du[i] + dtd5 * dT[i] + (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]);
   SOLVE(k5);
   for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a61) * k1[i] + RPC(a62) * k2[i] + RPC(a63) * k3[i] + RPC(a64) * k4[i] + RPC(a65) * k5[i];
-  model_f<float>(m, du, u, p, (float)(t + (Tt)dt));
+  model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
   for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC63 * k3[i] + dtC64 * k4[i] + dtC65 * k5[i]);
   SOLVE(k6);
   for (int i = 0; i < N; i++) u[i] = u[i] + k6[i];
-  model_f<float>(m, du, u, p, (float)(t + (Tt)dt));
+  model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
   for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC71 * k1[i] + dtC72 * k2[i] + dtC73 * k3[i] + dtC74 * k4[i] + dtC75 * k5[i] + dtC76 * k6[i]);
   SOLVE(k7);
   for (int i = 0; i < N; i++) u[i] = u[i] + k7[i];
-  model_f<float>(m, du, u, p, (float)(t + (Tt)dt));
+  model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
   for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC81 * k1[i] + dtC82 * k2[i] + dtC83 * k3[i] + dtC84 * k4[i] + dtC85 * k5[i] + dtC86 * k6[i] + dtC87 * k7[i]);
   SOLVE(k8);
 #undef SOLVE
@@ -630,16 +669,17 @@ static void interpolate(int m, int alg, const Integ<Tt>& ig, const float* p, flo
 /* ------------------------------------------------------------------ one trajectory (kernels.jl) */
 template <class Tt>
 static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* u0, const float* p, const double* tsp,
-                      Tt* ts, float* us, signed char* retcode, int* nacc, int* nrej) {
+                      typename TOut<Tt>::T* ts, float* us, signed char* retcode, int* nacc, int* nrej) {
+  typedef typename TOut<Tt>::T Out;
   ModelInfo mi = model_info(m);
   const int N = mi.N, L = cfg->L, alg = cfg->alg;
   Integ<Tt> ig;
   memset(&ig, 0, sizeof(ig));
   ig.N = N;
-  Tt t0 = (Tt)tsp[0], tf = (Tt)tsp[1];
+  Tt t0 = t_from<Tt>(tsp[0]), tf = t_from<Tt>(tsp[1]);
   for (int i = 0; i < N; i++) { ig.u[i] = u0[i]; ig.uprev[i] = u0[i]; for (int s = 0; s < 10; s++) ig.k[s][i] = u0[i]; }
   ig.t = t0; ig.tprev = t0; ig.tf = tf;
-  float dt_in = cfg->dt0 ? cfg->dt0[idx] : (float)(Tt)cfg->dt;
+  float dt_in = cfg->dt0 ? cfg->dt0[idx] : (float)cfg->dt;
   ig.dt = dt_in; ig.dtnew = dt_in;
   float tsc = cfg->tolscale ? cfg->tolscale[idx] : 1.0f;
   ig.abstol = cfg->abstol * tsc; ig.reltol = cfg->reltol * tsc;
@@ -648,22 +688,22 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
   ig.qold = C.qoldinit;
 
   /* fill! ts with tspan[1] (lowerlevel_solve.jl:82, 107, 318, 322) */
-  for (int l = 0; l < L; l++) ts[l] = t0;
+  for (int l = 0; l < L; l++) ts[l] = (Out)tsp[0];
   const double* sa = cfg->nsaveat ? (cfg->saveat_per_traj ? cfg->saveat + idx * cfg->nsaveat : cfg->saveat) : NULL;
   int nsa = cfg->nsaveat;
 #define US(l) (us + (size_t)(l) * N)
-#define SA(l) ((Tt)sa[(l)])
+#define SA(l) (t_from<Tt>(sa[(l)]))
   /* kernels.jl:35-47 / :116-126 (0-based cur_t here == 1-based cur_t - 1) */
   ig.cur_t = 0; ig.step_idx = 0;
   if (sa) {
-    if (t0 == SA(0)) { ig.cur_t = 1; for (int i = 0; i < N; i++) US(0)[i] = u0[i]; }
+    if ((Out)tsp[0] == (Out)sa[0]) { ig.cur_t = 1; for (int i = 0; i < N; i++) US(0)[i] = u0[i]; }
   } else {
-    ts[0] = t0; for (int i = 0; i < N; i++) US(0)[i] = u0[i];
+    ts[0] = (Out)tsp[0]; for (int i = 0; i < N; i++) US(0)[i] = u0[i];
   }
   ig.step_idx = 1;
 
   const int save_every = cfg->save_everystep && !cfg->adaptive; /* adaptive init stores save_everystep=false (types.jl) */
-  while (ig.t < tf && ig.retcode != RET_TERMINATED && ig.retcode != RET_DTMIN && ig.retcode != RET_MAXITERS) {
+  while (t_lt(ig.t, tf) && ig.retcode != RET_TERMINATED && ig.retcode != RET_DTMIN && ig.retcode != RET_MAXITERS) {
     /* ---------------- step! ---------------- */
     Tt t = ig.t;
     for (int i = 0; i < N; i++) ig.uprev[i] = ig.u[i];
@@ -671,11 +711,11 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
       if (++ig.nattempt > cfg->maxiters) { ig.retcode = RET_MAXITERS; break; }
       float dt = ig.dt;
       ig.tprev = t;
-      ig.t = t + (Tt)dt;
+      ig.t = t_add(t, dt);
       float u[MAXN];
       if (alg == ALG_TSIT5) {
         float k1[MAXN];
-        if (ig.u_modified) { model_f<float>(m, k1, ig.uprev, p, (float)t); ig.u_modified = 0; }
+        if (ig.u_modified) { model_f<float>(m, k1, ig.uprev, p, t_f32(t)); ig.u_modified = 0; }
         else for (int i = 0; i < N; i++) k1[i] = ig.k[6][i];
         tsit5_stages(m, ig, p, t, dt, k1, u, ig.k, 1);
       } else if (alg == ALG_VERN7) {
@@ -685,8 +725,8 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
         rb23_attempt(m, cfg->jac, ig, p, t, dt, u, ig.k[0], ig.k[1], err, 0);
       } else if (alg == ALG_RODAS5P) {
         float k8[MAXN];
-        compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, (float)t);
-        compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, (float)t);
+        compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, t_f32(t));
+        compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, t_f32(t));
         rodas5p_attempt(m, ig, p, t, dt, u, k8, ig.k);
       }
       for (int i = 0; i < N; i++) ig.u[i] = u[i];
@@ -695,12 +735,12 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
       float dt = ig.dtnew;
       float k1[MAXN];
       if (alg == ALG_TSIT5) {
-        if (ig.u_modified) { model_f<float>(m, k1, ig.uprev, p, (float)t); ig.u_modified = 0; }
+        if (ig.u_modified) { model_f<float>(m, k1, ig.uprev, p, t_f32(t)); ig.u_modified = 0; }
         else for (int i = 0; i < N; i++) k1[i] = ig.k[6][i];
       }
       if (alg == ALG_RODAS5P) { /* J, dT once per step, outside the reject loop (:182-186) */
-        compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, (float)t);
-        compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, (float)t);
+        compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, t_f32(t));
+        compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, t_f32(t));
       }
       float EEst = INFINITY;
       while (EEst > 1.0f) {
@@ -734,28 +774,28 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
     }
     /* ---------------- savevalues! (integrator_utils.jl:13-50) ---------------- */
     if (!sa && save_every) {
-      if (ig.step_idx < L) { for (int i = 0; i < N; i++) US(ig.step_idx)[i] = ig.u[i]; ts[ig.step_idx] = ig.t; }
+      if (ig.step_idx < L) { for (int i = 0; i < N; i++) US(ig.step_idx)[i] = ig.u[i]; ts[ig.step_idx] = t_out(ig.t); }
       ig.step_idx++;
     } else if (sa) {
-      while (ig.cur_t < nsa && SA(ig.cur_t) <= ig.t) {
+      while (ig.cur_t < nsa && t_le(SA(ig.cur_t), ig.t)) {
         Tt savet = SA(ig.cur_t);
-        float th = (float)((savet - ig.tprev) / (Tt)ig.dt);
-        if (ig.cur_t < L) { interpolate(m, alg, ig, p, th, ig.dt, US(ig.cur_t)); ts[ig.cur_t] = savet; }
+        float th = t_theta(savet, ig.tprev, ig.dt);
+        if (ig.cur_t < L) { interpolate(m, alg, ig, p, th, ig.dt, US(ig.cur_t)); ts[ig.cur_t] = (Out)sa[ig.cur_t]; }
         ig.cur_t++;
       }
     }
   }
   /* kernels.jl:53-62 / :133-142 */
-  if (ig.t > tf && !sa) {
-    if (!(!cfg->save_everystep)) { /* with !save_everystep slot 2 is overwritten right below */
-      float th = (float)((tf - ig.tprev) / (Tt)ig.dt);
+  if (t_lt(tf, ig.t) && !sa) {
+    if (cfg->save_everystep) { /* with !save_everystep slot 2 is overwritten right below */
+      float th = t_theta(tf, ig.tprev, ig.dt);
       interpolate(m, alg, ig, p, th, ig.dt, US(L - 1));
-      ts[L - 1] = tf;
+      ts[L - 1] = (Out)tsp[1];
     }
   }
   if (!sa && !cfg->save_everystep) {
     for (int i = 0; i < N; i++) US(1)[i] = ig.u[i];
-    ts[1] = ig.t;
+    ts[1] = t_out(ig.t);
   }
 #undef US
 #undef SA
@@ -794,45 +834,46 @@ static void normals4(uint64_t seed, uint32_t step, uint32_t traj, uint32_t blk, 
 }
 
 template <class Tt>
-static void em_one(int m, const oracle_cfg* cfg, long long idx, const float* u0, const float* p, const double* tsp, Tt* ts, float* us, signed char* retcode) {
+static void em_one(int m, const oracle_cfg* cfg, long long idx, const float* u0, const float* p, const double* tsp,
+                   typename TOut<Tt>::T* ts, float* us, signed char* retcode) {
+  typedef typename TOut<Tt>::T Out;
   ModelInfo mi = model_info(m);
   const int N = mi.N, L = cfg->L;
-  Tt t0 = (Tt)tsp[0], tf = (Tt)tsp[1];
-  Tt dtT = (Tt)cfg->dt;
-  float dt = (float)dtT;
-  for (int l = 0; l < L; l++) ts[l] = t0;
+  const Out t0_in = (Out)tsp[0], tf_in = (Out)tsp[1];
+  const float dt = (float)cfg->dt;
+  for (int l = 0; l < L; l++) ts[l] = t0_in;
   const double* sa = cfg->nsaveat ? (cfg->saveat_per_traj ? cfg->saveat + idx * cfg->nsaveat : cfg->saveat) : NULL;
   int nsa = cfg->nsaveat, cur_t = 0;
 #define US(l) (us + (size_t)(l) * N)
-  if (sa) { if (t0 == (Tt)sa[0]) { cur_t = 1; for (int i = 0; i < N; i++) US(0)[i] = u0[i]; } }
-  else { ts[0] = t0; for (int i = 0; i < N; i++) US(0)[i] = u0[i]; }
+  if (sa) { if (t0_in == (Out)sa[0]) { cur_t = 1; for (int i = 0; i < N; i++) US(0)[i] = u0[i]; } }
+  else { ts[0] = t0_in; for (int i = 0; i < N; i++) US(0)[i] = u0[i]; }
   float sqdt = sqrtf(dt);
   float u[MAXN], up[MAXN], f[MAXN], g[MAXN], z[MAXN + 4];
   for (int i = 0; i < N; i++) u[i] = u0[i];
-  Tt t = t0;
-  Tt span = tf - t0;
-  Tt ratio = (span < 0 ? -span : span) / (dtT < 0 ? -dtT : dtT); /* floor(Int, abs(tf - t0) / abs(dt)) in Tt */
+  Tt t = t_from<Tt>(tsp[0]);
+  const Out span = tf_in - t0_in, dtb = (Out)dt;
+  const Out ratio = (span < 0 ? -span : span) / (dtb < 0 ? -dtb : dtb); /* floor(Int, abs(tf - t0) / abs(dt)) */
   long long n = (long long)floor((double)ratio) + 1;
   if (n - 1 > cfg->maxiters) n = cfg->maxiters + 1;
   for (long long j = 2; j <= n; j++) {
     for (int i = 0; i < N; i++) up[i] = u[i];
-    model_f<float>(m, f, up, p, (float)t);
+    model_f<float>(m, f, up, p, t_f32(t));
     model_g(m, g, up, p);
     for (int b = 0; b < (N + 3) / 4; b++) normals4(cfg->seed, (uint32_t)(j - 2), (uint32_t)idx, (uint32_t)b, z + 4 * b);
     for (int i = 0; i < N; i++) u[i] = up[i] + f[i] * dt + (sqdt * g[i]) * z[i];
-    t = t + (Tt)dt;
+    t = t_add(t, dt);
     if (!sa && cfg->save_everystep) {
-      if (j - 1 < L) { for (int i = 0; i < N; i++) US(j - 1)[i] = u[i]; ts[j - 1] = t; }
+      if (j - 1 < L) { for (int i = 0; i < N; i++) US(j - 1)[i] = u[i]; ts[j - 1] = t_out(t); }
     } else if (sa) {
-      while (cur_t < nsa && (Tt)sa[cur_t] <= t) {
-        Tt savet = (Tt)sa[cur_t];
-        float th = (float)((savet - (t - (Tt)dt)) / (Tt)dt);
-        if (cur_t < L) { for (int i = 0; i < N; i++) US(cur_t)[i] = up[i] + (u[i] - up[i]) * th; ts[cur_t] = savet; }
+      while (cur_t < nsa && t_le(t_from<Tt>(sa[cur_t]), t)) {
+        Tt savet = t_from<Tt>(sa[cur_t]);
+        float th = t_em_theta(savet, t, dt);
+        if (cur_t < L) { for (int i = 0; i < N; i++) US(cur_t)[i] = up[i] + (u[i] - up[i]) * th; ts[cur_t] = (Out)sa[cur_t]; }
         cur_t++;
       }
     }
   }
-  if (!sa && !cfg->save_everystep) { for (int i = 0; i < N; i++) US(1)[i] = u[i]; ts[1] = t; }
+  if (!sa && !cfg->save_everystep) { for (int i = 0; i < N; i++) US(1)[i] = u[i]; ts[1] = t_out(t); }
 #undef US
   int finite = 1;
   for (int i = 0; i < N; i++) if (!isfinite(u[i])) finite = 0;
@@ -866,10 +907,10 @@ int oracle_solve(int model, long long B, const float* u0, const float* p, const 
     const double* tsp = tspan + 2 * (size_t)i;
     float* usi = us + (size_t)i * L * N;
     if (cfg->alg == ALG_EM) {
-      if (cfg->time_f64) em_one<double>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (double*)ts + (size_t)i * L, usi, retcode);
+      if (cfg->time_f64) em_one<DF>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (double*)ts + (size_t)i * L, usi, retcode);
       else em_one<float>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (float*)ts + (size_t)i * L, usi, retcode);
     } else {
-      if (cfg->time_f64) solve_one<double>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (double*)ts + (size_t)i * L, usi, retcode, naccept, nreject);
+      if (cfg->time_f64) solve_one<DF>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (double*)ts + (size_t)i * L, usi, retcode, naccept, nreject);
       else solve_one<float>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (float*)ts + (size_t)i * L, usi, retcode, naccept, nreject);
     }
   }
