@@ -70,6 +70,7 @@ struct Driver {
   CUresult (*FuncGetAttribute)(int*, CUfunction_attribute, CUfunction) = nullptr;
   CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
   CUresult (*GetErrorString)(CUresult, const char**) = nullptr;
+  CUresult (*FuncSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
   bool ok = false;
 };
 Driver g_drv;
@@ -92,7 +93,8 @@ int load_driver() {
     bool ok = resolve("cuModuleLoadData", g_drv.ModuleLoadData) && resolve("cuModuleGetFunction", g_drv.ModuleGetFunction) &&
               resolve("cuLaunchKernel", g_drv.LaunchKernel) && resolve("cuFuncGetAttribute", g_drv.FuncGetAttribute) &&
               resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", g_drv.OccupancyMaxActiveBlocksPerMultiprocessor) &&
-              resolve("cuGetErrorString", g_drv.GetErrorString);
+              resolve("cuGetErrorString", g_drv.GetErrorString) &&
+              resolve("cuFuncSetAttribute", g_drv.FuncSetAttribute);
     if (!ok) err = "could not resolve CUDA driver entry points";
     g_drv.ok = ok;
   });
@@ -342,6 +344,7 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   P.retcode = out->retcode;
   P.naccept = out->naccept;
   P.nreject = out->nreject;
+  P.dt_first = out->dt_first;
   P.dt0 = o->dt0;
   P.tolscale = o->tolscale;
   P.B = pr->B;
@@ -367,12 +370,36 @@ int sm_count() {
   return n > 0 ? n : 1;
 }
 
+// Dynamic shared memory of the ODE drivers: the shared saveat grid (once per block, in the
+// kernels' time type) and, when they fit, one staged output column of L*N floats per lane.
+struct SmemCfg {
+  int shared_saveat = 0, stage_cols = 0;
+  size_t bytes = 0;
+};
+SmemCfg smem_for(const Request& rq, int block, int N) {
+  SmemCfg c;
+  const degpu_kparams& P = rq.kp;
+  if (rq.spec.driver == 3 || P.nsaveat == 0) return c;
+  const size_t tsz = rq.spec.tt ? 8 : 4;
+  if (!P.saveat_per_traj && (size_t)P.nsaveat * tsz <= 16384) {
+    c.shared_saveat = 1;
+    c.bytes = ((size_t)P.nsaveat * tsz + 15) & ~(size_t)15;
+  }
+  const size_t cols = (size_t)block * P.L * N * sizeof(float);
+  if (!getenv("DEGPU_NO_STAGING") && cols <= 96 * 1024) {
+    c.stage_cols = 1;
+    c.bytes += cols;
+  }
+  return c;
+}
+
 int grid_for(const Request& rq, const Kernel& K, int block) {
   long long B = rq.kp.B;
   if (rq.spec.driver != 2) return (int)((B + block - 1) / block);
   // persistent: fill the machine once (a multiple of the SM count), never more than needed
   int per_sm = 0;
-  g_drv.OccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, K.fn, block, 0);
+  const SmemCfg sc = smem_for(rq, block, rq.f->N);
+  g_drv.OccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, K.fn, block, sc.bytes);
   if (per_sm < 1) per_sm = 1;
   long long g = (long long)per_sm * sm_count();
   long long need = (B + block - 1) / block;
@@ -386,13 +413,18 @@ int launch(const Request& rq, const Kernel& K, int block, int chunk, unsigned lo
   degpu_kparams P = rq.kp;
   P.chunk = chunk;
   P.work = work;
+  const SmemCfg sc = smem_for(rq, block, rq.f->N);
+  P.shared_saveat = sc.shared_saveat;
+  P.stage_cols = sc.stage_cols;
+  if (sc.bytes > 48 * 1024)
+    CU_TRY(g_drv.FuncSetAttribute(K.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)sc.bytes));
   int grid = grid_for(rq, K, block);
   if (rq.spec.driver == 2) {
     if (!work) return fail(DEGPU_E_INVALID, "persistent driver without a work counter");
     CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(unsigned long long), (cudaStream_t)s));
   }
   void* args[] = {(void*)&P};
-  CU_TRY(g_drv.LaunchKernel(K.fn, grid, 1, 1, block, 1, 1, 0, s, args, nullptr));
+  CU_TRY(g_drv.LaunchKernel(K.fn, grid, 1, 1, block, 1, 1, (unsigned)sc.bytes, s, args, nullptr));
   return 0;
 }
 
@@ -508,7 +540,7 @@ int degpu_batch_solve_host(const degpu_rhs* f, const float* u0, const float* p, 
     degpu_options o = *opt;
     if (n_sa) o.saveat = d + off_sa;
     degpu_outputs out{d + off_ts, (float*)(d + off_us), L, retcode ? (signed char*)(d + off_rc) : nullptr,
-                      naccept ? (int*)(d + off_na) : nullptr, nreject ? (int*)(d + off_nr) : nullptr};
+                      naccept ? (int*)(d + off_na) : nullptr, nreject ? (int*)(d + off_nr) : nullptr, nullptr};
     rc = (opt->alg == DEGPU_ALG_EM) ? degpu_vectorized_solve_sde(f, &pr, &o, &out, s)
                                     : (adaptive ? degpu_vectorized_asolve(f, &pr, &o, &out, s)
                                                 : degpu_vectorized_solve(f, &pr, &o, &out, s));
@@ -532,7 +564,7 @@ int degpu_rhs_check(const degpu_rhs* f, const degpu_options* opt, int adaptive, 
   if (!f || !opt) return fail(DEGPU_E_INVALID, "null argument");
   Request rq;
   degpu_problems pr{nullptr, nullptr, nullptr, 0};
-  degpu_outputs out{nullptr, nullptr, opt->nsaveat ? opt->nsaveat : 2, nullptr, nullptr, nullptr};
+  degpu_outputs out{nullptr, nullptr, opt->nsaveat ? opt->nsaveat : 2, nullptr, nullptr, nullptr, nullptr};
   degpu_options o = *opt;
   if (!(o.dt > 0)) o.dt = 1.0;
   if (!o.nsaveat) o.save_everystep = 0;
@@ -550,7 +582,7 @@ int degpu_kernel_info(const degpu_rhs* f, const degpu_options* opt, int adaptive
   if (!f || !opt) return fail(DEGPU_E_INVALID, "null argument");
   Request rq;
   degpu_problems pr{nullptr, nullptr, nullptr, 0};
-  degpu_outputs out{nullptr, nullptr, opt->nsaveat ? opt->nsaveat : 2, nullptr, nullptr, nullptr};
+  degpu_outputs out{nullptr, nullptr, opt->nsaveat ? opt->nsaveat : 2, nullptr, nullptr, nullptr, nullptr};
   degpu_options o = *opt;
   if (!(o.dt > 0)) o.dt = 1.0;
   int rc = make_request(f, &pr, &o, adaptive, &out, &rq);

@@ -691,20 +691,71 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 
 #if DEGPU_ALG <= 3
 // ------------------------------------------------------------------ driver pieces (kernels.jl)
+// Output and saveat access of one lane.  With staging on (saveat runs whose L*N columns
+// fit in shared memory), saved rows go to the lane's column in shared memory and the warp
+// writes whole finished columns to HBM with coalesced stores (flush_columns); otherwise
+// rows are stored straight to global memory.  A shared saveat grid is converted to the
+// internal time type once per block (sa_s) instead of once per save.
 struct Io {
   const degpu_kparams& P;
+  float* col;          // this lane's staged column (L*N floats) or nullptr
+  const Time* sa_s;    // shared saveat grid in shared memory, or nullptr
   DEGPU_DEV Tt* ts(long long i) const { return (Tt*)P.ts + i * P.L; }
   DEGPU_DEV float* us(long long i) const { return P.us + i * (long long)P.L * N; }
   DEGPU_DEV Tt saveat(long long i, int l) const {
     const Tt* s = (const Tt*)P.saveat;
     return P.saveat_per_traj ? s[i * P.nsaveat + l] : __ldg(s + l);
   }
+  DEGPU_DEV Time save_time(long long i, int l) const { return sa_s ? sa_s[l] : TP::from(saveat(i, l)); }
   DEGPU_DEV void store_u(long long i, int l, const float* v) const {
-    float* dst = us(i) + (long long)l * N;
+    float* dst = col ? col + l * N : us(i) + (long long)l * N;
 #pragma unroll
     for (int c = 0; c < N; c++) dst[c] = v[c];
   }
 };
+
+// Shared-memory layout of the adaptive drivers: [saveat grid (Time) | staged columns].
+struct SmemPlan {
+  const Time* sa_s;
+  float* cols;
+};
+DEGPU_DEV SmemPlan setup_smem(const degpu_kparams& P, char* smem) {
+  SmemPlan sp{nullptr, nullptr};
+  size_t off = 0;
+  if (P.nsaveat && !P.saveat_per_traj && P.shared_saveat) {
+    Time* t = reinterpret_cast<Time*>(smem);
+    const Tt* s = (const Tt*)P.saveat;
+    for (int l = threadIdx.x; l < P.nsaveat; l += blockDim.x) t[l] = TP::from(s[l]);
+    sp.sa_s = t;
+    off = ((size_t)P.nsaveat * sizeof(Time) + 15) & ~(size_t)15;
+  }
+  if (P.stage_cols) sp.cols = reinterpret_cast<float*>(smem + off);
+  __syncthreads();
+  return sp;
+}
+
+// Warp-cooperative write of the finished lanes' staged columns (mask) and their ts
+// columns: 32 lanes store consecutive words of one trajectory's contiguous column.
+DEGPU_DEV void flush_columns(const Io& io, const float* warp_cols, unsigned mask, long long my, int my_cur, Tt my_t0) {
+  const degpu_kparams& P = io.P;
+  const int lane = threadIdx.x & 31;
+  const int LN = P.L * N;
+  __syncwarp();
+  while (mask) {
+    const int b = __ffs(mask) - 1;
+    mask &= mask - 1;
+    const long long tr = __shfl_sync(0xffffffffu, my, b);
+    const int cur = __shfl_sync(0xffffffffu, my_cur, b);
+    const Tt t0 = __shfl_sync(0xffffffffu, my_t0, b);
+    const float* src = warp_cols + b * LN;
+    float* dst = P.us + tr * (long long)LN;
+    for (int k = lane; k < LN; k += 32)
+      if (k < cur * N) dst[k] = src[k];  // rows never saved stay untouched, like the reference's
+    Tt* ts = (Tt*)P.ts + tr * P.L;
+    for (int l = lane; l < P.L; l += 32) ts[l] = (l < cur) ? io.saveat(tr, l) : t0;
+  }
+  __syncwarp();
+}
 
 // init (nonstiff/types.jl:340-402 et al.) + initial save (kernels.jl:116-126)
 DEGPU_DEV void lane_init(Lane& L, const Io& io, long long i) {
@@ -741,7 +792,7 @@ DEGPU_DEV void lane_init(Lane& L, const Io& io, long long i) {
   if (P.nsaveat) {
     const Tt s0 = io.saveat(i, 0);
     if (t0_in == s0) { L.cur_t = 1; io.store_u(i, 0, L.u); }
-    L.next_save = TP::from(L.cur_t < P.nsaveat ? io.saveat(i, L.cur_t) : s0);
+    L.next_save = io.save_time(i, L.cur_t < P.nsaveat ? L.cur_t : 0);
   } else {
     io.store_u(i, 0, L.u);
   }
@@ -760,7 +811,7 @@ DEGPU_DEV void save_values(Lane& L, const Io& io, long long i, bool save_everyst
         io.store_u(i, L.cur_t, v);
       }
       L.cur_t++;
-      if (L.cur_t < P.nsaveat) L.next_save = TP::from(io.saveat(i, L.cur_t));
+      if (L.cur_t < P.nsaveat) L.next_save = io.save_time(i, L.cur_t);
     }
   } else if (save_everystep) {
     if (L.step_idx < P.L) { io.store_u(i, L.step_idx, L.u); io.ts(i)[L.step_idx] = TP::out(L.t); }
@@ -814,6 +865,7 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, long long i) {
       L.nreject++;
       return false;
     }
+    if (L.naccept == 0 && P.dt_first) P.dt_first[i] = dt;
   } else {
     if (++L.nattempt > P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
     float dt = L.dt;
@@ -835,7 +887,8 @@ DEGPU_DEV void lane_finish(Lane& L, const Io& io, long long i) {
   Tt* ts = io.ts(i);
   const Tt t0_in = ((const Tt*)P.tspan)[2 * i];  // fill! ts with tspan[1] (lowerlevel_solve.jl:82)
   if (P.nsaveat) {
-    for (int l = 0; l < P.L; l++) ts[l] = (l < L.cur_t) ? io.saveat(i, l) : t0_in;
+    if (!io.col)  // staged columns are written by flush_columns
+      for (int l = 0; l < P.L; l++) ts[l] = (l < L.cur_t) ? io.saveat(i, l) : t0_in;
   } else {
     int first_unset = P.save_everystep ? (L.step_idx < P.L ? L.step_idx : P.L) : 1;
     ts[0] = t0_in;
@@ -867,14 +920,23 @@ DEGPU_DEV void lane_finish(Lane& L, const Io& io, long long i) {
 // ode_solve_kernel / ode_asolve_kernel (kernels.jl:1-152): one trajectory per thread.
 extern "C" __global__ void __launch_bounds__(256) degpu_solve_kernel(const degpu_kparams P) {
   using namespace degpu;
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P.B) return;
-  Io io{P};
+  extern __shared__ __align__(16) char smem[];
+  const SmemPlan sp = setup_smem(P, smem);
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < P.B;
+  float* warp_cols = sp.cols ? sp.cols + (threadIdx.x & ~31) * P.L * N : nullptr;
+  Io io{P, sp.cols ? warp_cols + (threadIdx.x & 31) * P.L * N : nullptr, sp.sa_s};
   Lane L;
-  lane_init(L, io, i);
-  bool done = !TP::lt(L.t, L.tf);
-  while (!done) done = advance<DEGPU_DRIVER == 1>(L, io, i);
-  lane_finish(L, io, i);
+  if (valid) {
+    lane_init(L, io, i);
+    bool done = !TP::lt(L.t, L.tf);
+    while (!done) done = advance<DEGPU_DRIVER == 1>(L, io, i);
+    lane_finish(L, io, i);
+  }
+  if (sp.cols) {
+    const unsigned m = __ballot_sync(0xffffffffu, valid);
+    flush_columns(io, warp_cols, m, i, valid ? L.cur_t : 0, valid ? ((const Tt*)P.tspan)[2 * i] : (Tt)0);
+  }
 }
 #endif
 
@@ -891,7 +953,10 @@ extern "C" __global__ void __launch_bounds__(256) degpu_persistent_kernel(const 
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
-  Io io{P};
+  extern __shared__ __align__(16) char smem[];
+  const SmemPlan sp = setup_smem(P, smem);
+  float* warp_cols = sp.cols ? sp.cols + (threadIdx.x & ~31) * P.L * N : nullptr;
+  Io io{P, sp.cols ? warp_cols + lane * P.L * N : nullptr, sp.sa_s};
   Lane L;
   long long my = -1;
   long long q_next = 0, q_end = 0;
@@ -899,6 +964,7 @@ extern "C" __global__ void __launch_bounds__(256) degpu_persistent_kernel(const 
   const long long B = P.B;
   const int chunk = P.chunk > 0 ? P.chunk : 32;
   for (;;) {
+    bool fin = false;
     unsigned idle = __ballot_sync(FULL, my < 0);
     if (idle) {
       if (q_next >= q_end && !exhausted) {
@@ -912,17 +978,19 @@ extern "C" __global__ void __launch_bounds__(256) degpu_persistent_kernel(const 
       if (my < 0 && q_next + rank < q_end) {
         my = q_next + rank;
         lane_init(L, io, my);
-        if (!TP::lt(L.t, L.tf)) { lane_finish(L, io, my); my = -1; }
+        if (!TP::lt(L.t, L.tf)) { lane_finish(L, io, my); fin = true; }
       }
       q_next = min(q_next + (long long)__popc(idle), q_end);
     }
-    if (__ballot_sync(FULL, my >= 0) == 0) {
-      if (exhausted) break;
-      continue;
+    if (my >= 0 && !fin) {
+      if (advance<true>(L, io, my)) { lane_finish(L, io, my); fin = true; }
     }
-    if (my >= 0) {
-      if (advance<true>(L, io, my)) { lane_finish(L, io, my); my = -1; }
+    if (sp.cols) {
+      const unsigned fm = __ballot_sync(FULL, fin);
+      if (fm) flush_columns(io, warp_cols, fm, my, fin ? L.cur_t : 0, fin ? ((const Tt*)P.tspan)[2 * my] : (Tt)0);
     }
+    if (fin) my = -1;
+    if (__ballot_sync(FULL, my >= 0) == 0 && exhausted) break;
   }
 }
 #endif

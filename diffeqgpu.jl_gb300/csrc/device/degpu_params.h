@@ -31,6 +31,7 @@ typedef struct degpu_kparams {
   int* nreject;           /* [B] or null */
   const float* dt0;       /* [B] per-trajectory initial dt (learned controller) or null */
   const float* tolscale;  /* [B] per-trajectory tolerance multiplier (learned controller) or null */
+  float* dt_first;         /* [B] or null: first accepted dt (step-size trace) */
   unsigned long long* work; /* persistent driver: work[0] = next unclaimed trajectory */
   long long B;
   long long maxiters;     /* cap on step attempts per trajectory */
@@ -44,6 +45,8 @@ typedef struct degpu_kparams {
   int saveat_per_traj;
   int save_everystep;
   int chunk;              /* persistent driver: trajectories claimed per warp refill */
+  int stage_cols;         /* saved rows staged per lane in shared memory (blockDim*L*N floats) */
+  int shared_saveat;      /* shared saveat grid converted once per block into shared memory */
   int pad_;
 } degpu_kparams;
 

@@ -190,9 +190,17 @@ DEGPU_DEV void pm_sincos_turns(float v, float* s, float* c) {
   else { *s = -cr; *c = sr; }
 }
 
-// Julia's Base.min/max for floats propagate NaN (fminf/fmaxf would drop it)
+// Julia's Base.min/max for floats propagate NaN (fminf/fmaxf would drop it).  Parity mode
+// keeps that; fast mode uses the single-instruction min/max: a NaN state then reaches the
+// end of the span with finite step sizes instead of a NaN step size, and still ends with
+// retcode Unstable.
+#if DEGPU_PARITY
 DEGPU_DEV float jl_min(float x, float y) { if (x != x) return x; if (y != y) return y; return y < x ? y : x; }
 DEGPU_DEV float jl_max(float x, float y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
+#else
+DEGPU_DEV float jl_min(float x, float y) { return fminf(x, y); }
+DEGPU_DEV float jl_max(float x, float y) { return fmaxf(x, y); }
+#endif
 DEGPU_DEV double jl_mind(double x, double y) { if (x != x) return x; if (y != y) return y; return y < x ? y : x; }
 
 }  // namespace degpu

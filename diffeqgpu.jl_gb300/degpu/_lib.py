@@ -35,7 +35,8 @@ class Options(ctypes.Structure):
 
 class Outputs(ctypes.Structure):
     _fields_ = [("ts", ctypes.c_void_p), ("us", ctypes.c_void_p), ("L", ctypes.c_int),
-                ("retcode", ctypes.c_void_p), ("naccept", ctypes.c_void_p), ("nreject", ctypes.c_void_p)]
+                ("retcode", ctypes.c_void_p), ("naccept", ctypes.c_void_p), ("nreject", ctypes.c_void_p),
+                ("dt_first", ctypes.c_void_p)]
 
 
 class DegpuError(RuntimeError):
@@ -70,6 +71,16 @@ SIGNATURES = {
                                       ctypes.POINTER(ctypes.c_int)]),
     "degpu_rhs_check": (ctypes.c_int, [_P, ctypes.POINTER(Options), ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
     "degpu_fp32_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), _P]),
+    "degpu_mlp_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(_P)]),
+    "degpu_mlp_destroy": (None, [_P]),
+    "degpu_mlp_param_count": (ctypes.c_int, [_P]),
+    "degpu_mlp_set_params": (ctypes.c_int, [_P, _P, _P, _P]),
+    "degpu_mlp_get_params": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "degpu_mlp_infer": (ctypes.c_int, [_P, _P, ctypes.c_longlong, _P, _P, _P, ctypes.c_float, ctypes.c_float,
+                                       ctypes.c_float, ctypes.c_float, _P]),
+    "degpu_mlp_grad": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_longlong, _P, _P]),
+    "degpu_mlp_adam_step": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                           ctypes.c_float, _P]),
     "degpu_kernel_info": (ctypes.c_int, [_P, ctypes.POINTER(Options), ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                          ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
 }

@@ -381,10 +381,11 @@ class KernelResult:
     retcode: Any   # torch (B,) int8
     naccept: Any   # torch (B,) int32
     nreject: Any   # torch (B,) int32
+    dt_first: Any = None  # torch (B,) f32: first accepted dt (trace=True)
 
 
 def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None, save_everystep=None,
-                  abstol=1e-6, reltol=1e-3, stream=None, stats=True, **kw) -> KernelResult:
+                  abstol=1e-6, reltol=1e-3, stream=None, stats=True, trace=False, **kw) -> KernelResult:
     import torch
     f = probs.f
     Tt = probs.Tt
@@ -416,6 +417,7 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
     rc = torch.zeros(B, dtype=torch.int8, device=dev)
     na = torch.zeros(B, dtype=torch.int32, device=dev) if stats else None
     nr = torch.zeros(B, dtype=torch.int32, device=dev) if stats else None
+    dtf = torch.zeros(B, dtype=torch.float32, device=dev) if trace else None
     dt0 = kw.pop("dt0", None)
     tolscale = kw.pop("tolscale", None)
     opt = _options(alg, Tt, dt=dt, abstol=abstol, reltol=reltol, save_everystep=save_everystep,
@@ -424,7 +426,7 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
                    dt0=None if dt0 is None else dt0.data_ptr(),
                    tolscale=None if tolscale is None else tolscale.data_ptr(), **kw)
     out = _lib.Outputs(ts.data_ptr(), us.data_ptr(), L, rc.data_ptr(), None if na is None else na.data_ptr(),
-                       None if nr is None else nr.data_ptr())
+                       None if nr is None else nr.data_ptr(), None if dtf is None else dtf.data_ptr())
     st = stream if stream is not None else torch.cuda.current_stream(dev)
     pr = probs.cstruct()
     with torch.cuda.device(dev):
@@ -435,7 +437,7 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
         else:
             fn = lib().degpu_vectorized_solve
         check(fn(f.handle(), ctypes.byref(pr), ctypes.byref(opt), ctypes.byref(out), ctypes.c_void_p(st.cuda_stream)))
-    return KernelResult(ts, us, rc, na, nr)
+    return KernelResult(ts, us, rc, na, nr, dtf)
 
 
 def vectorized_solve(probs: DeviceProblems, prob: ODEProblem, alg, *, dt, saveat=None, save_everystep=True,

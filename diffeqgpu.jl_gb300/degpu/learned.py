@@ -1,0 +1,194 @@
+"""Learned step control: a BF16 MLP predicting each trajectory's initial dt and tolerance
+scale from (u0, p, log10 reltol), trained on the GPU by libdegpu's own kernels on traces
+that the plain solver generates.  No counterpart in the reference.
+
+Targets, from two plain solves of the training ensemble (both on the GPU):
+  * log dt0    -- the first step the plain controller accepted (accepted-step trace);
+  * log scale  -- how far the trajectory's tolerances can be relaxed before its final-state
+    error reaches a common target: err_i is the plain solution's distance to a 32x
+    tighter plain solve, scale_i = clip((target / err_i)^(1/alpha), 1, s_max).  Scales
+    are >= 1: the learned run is never asked for tighter tolerances than the plain run,
+    and members whose error already exceeds the target (chaotic ones) keep the plain
+    tolerances.  The embedded error estimate still accepts or rejects every step.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+N_OUT = 2
+
+
+def _sigs():
+    """Signatures live in _lib.SIGNATURES; kept for callers that registered them explicitly."""
+    lib()
+
+
+def features(u0, p, reltol):
+    """x = (u0, p, log10 reltol) per trajectory, float32 [B, N + P + 1]."""
+    u0 = np.asarray(u0, np.float32)
+    p = np.asarray(p, np.float32).reshape(u0.shape[0], -1)
+    lt = np.broadcast_to(np.log10(np.asarray(reltol, np.float64)), (u0.shape[0],)).astype(np.float32)
+    return np.concatenate([u0, p, lt[:, None]], axis=1).astype(np.float32)
+
+
+class StepSizeModel:
+    """libdegpu's BF16 MLP (degpu_mlp_*), device-resident."""
+
+    def __init__(self, n_in: int, seed: int = 0):
+        _sigs()
+        h = ctypes.c_void_p()
+        check(lib().degpu_mlp_create(n_in, seed, ctypes.byref(h)))
+        self.h = h
+        self.n_in = n_in
+        self.count = lib().degpu_mlp_param_count(h)
+        self.dt_range = (1e-8, 1e3)
+        self.scale_range = (1.0, 1e3)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None) is not None and _lib._lib is not None:
+                _lib._lib.degpu_mlp_destroy(self.h)
+        except Exception:
+            pass
+
+    # -------------------------------------------------------------- parameters
+    def get(self):
+        p = np.zeros(self.count, np.float32)
+        g = np.zeros(self.count, np.float32)
+        mu = np.zeros(self.n_in, np.float32)
+        sd = np.zeros(self.n_in, np.float32)
+        check(lib().degpu_mlp_get_params(self.h, p.ctypes.data, g.ctypes.data, mu.ctypes.data, sd.ctypes.data))
+        return p, g, mu, sd
+
+    def set(self, params=None, mean=None, std=None):
+        def ptr(a):
+            return None if a is None else np.ascontiguousarray(a, np.float32).ctypes.data
+        keep = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (params, mean, std)]
+        check(lib().degpu_mlp_set_params(self.h, *(None if a is None else a.ctypes.data for a in keep)))
+
+    def save(self, path):
+        p, _, mu, sd = self.get()
+        np.savez(path, params=p, mean=mu, std=sd, n_in=self.n_in, dt_range=self.dt_range, scale_range=self.scale_range)
+
+    @classmethod
+    def load(cls, path):
+        z = np.load(path)
+        m = cls(int(z["n_in"]))
+        m.set(z["params"], z["mean"], z["std"])
+        m.dt_range = tuple(z["dt_range"])
+        m.scale_range = tuple(z["scale_range"])
+        return m
+
+    # -------------------------------------------------------------- kernels
+    def grad(self, x_dev, t_dev, w_dev=None, stream=None):
+        import torch
+        st = stream or torch.cuda.current_stream()
+        loss = torch.zeros(1, dtype=torch.float32, device=x_dev.device)
+        check(lib().degpu_mlp_grad(self.h, x_dev.data_ptr(), t_dev.data_ptr(), None if w_dev is None else w_dev.data_ptr(),
+                                   x_dev.shape[0], loss.data_ptr(), ctypes.c_void_p(st.cuda_stream)))
+        return loss
+
+    def adam(self, lr, beta1=0.9, beta2=0.999, eps=1e-8, wd=0.0, stream=None):
+        import torch
+        st = stream or torch.cuda.current_stream()
+        check(lib().degpu_mlp_adam_step(self.h, lr, beta1, beta2, eps, wd, ctypes.c_void_p(st.cuda_stream)))
+
+    def infer(self, x_dev, raw=False, stream=None):
+        """Tensor-core inference.  Returns (dt0, tolscale) device tensors, or raw y [B,2]."""
+        import torch
+        st = stream or torch.cuda.current_stream()
+        B = x_dev.shape[0]
+        y = torch.empty((B, 2), dtype=torch.float32, device=x_dev.device) if raw else None
+        d0 = None if raw else torch.empty(B, dtype=torch.float32, device=x_dev.device)
+        sc = None if raw else torch.empty(B, dtype=torch.float32, device=x_dev.device)
+        check(lib().degpu_mlp_infer(self.h, x_dev.data_ptr(), B, None if y is None else y.data_ptr(),
+                                    None if d0 is None else d0.data_ptr(), None if sc is None else sc.data_ptr(),
+                                    self.dt_range[0], self.dt_range[1], self.scale_range[0], self.scale_range[1],
+                                    ctypes.c_void_p(st.cuda_stream)))
+        return y if raw else (d0, sc)
+
+    # -------------------------------------------------------------- training
+    def fit(self, x, targets, weights=None, *, epochs=8, batch=8192, lr=3e-3, seed=0, log=None):
+        """Adam on the weighted MSE; x, targets, weights are host arrays or device tensors."""
+        import torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+        x = torch.as_tensor(np.asarray(x, np.float32) if not torch.is_tensor(x) else x, device=dev)
+        t = torch.as_tensor(np.asarray(targets, np.float32) if not torch.is_tensor(targets) else targets, device=dev)
+        w = None if weights is None else torch.as_tensor(
+            np.asarray(weights, np.float32) if not torch.is_tensor(weights) else weights, device=dev)
+        mean = x.mean(0).cpu().numpy()
+        std = x.std(0).clamp_min(1e-6).cpu().numpy()
+        self.set(mean=mean, std=std)
+        n = x.shape[0]
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        hist = []
+        steps = max(1, epochs * ((n + batch - 1) // batch))
+        k = 0
+        for ep in range(epochs):
+            perm = torch.randperm(n, device=dev, generator=g)
+            tot = torch.zeros((), device=dev)
+            for b0 in range(0, n, batch):
+                idx = perm[b0:b0 + batch]
+                xb, tb = x[idx].contiguous(), t[idx].contiguous()
+                wb = None if w is None else w[idx].contiguous()
+                loss = self.grad(xb, tb, wb)
+                # cosine learning-rate decay
+                cur = lr * 0.5 * (1 + np.cos(np.pi * k / steps))
+                self.adam(cur)
+                tot += loss[0] * xb.shape[0]
+                k += 1
+            hist.append(float(tot) / n)
+            if log:
+                log(f"epoch {ep}: loss {hist[-1]:.5f}")
+        return hist
+
+
+def training_targets(first_dt, err, target_err, *, alpha=1.0, s_max=1e3, err_floor=1e-9):
+    """(log dt0, log scale) targets and weights from the plain solver's traces."""
+    first_dt = np.asarray(first_dt, np.float64)
+    err = np.maximum(np.asarray(err, np.float64), err_floor)
+    ok = np.isfinite(first_dt) & (first_dt > 0) & np.isfinite(err)
+    scale = np.clip((target_err / err) ** (1.0 / alpha), 1.0, s_max)
+    y = np.stack([np.log(np.where(ok, first_dt, 1.0)), np.log(scale)], 1).astype(np.float32)
+    w = np.stack([ok, ok], 1).astype(np.float32)
+    return y, w
+
+
+def solver_traces(f, u0, p, tspan, time_type, alg, *, reltol, abstol, dt=0.1, tighten=32.0, device=None, driver="persistent"):
+    """Run the plain solver twice (at the given tolerances and `tighten` x tighter) and return
+    (first accepted dt, final-state error proxy, naccept + nreject) per trajectory."""
+    import torch
+
+    from .api import DeviceProblems, _solve_device
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    B = u0.shape[0]
+    tsp = np.broadcast_to(np.asarray(tspan, dtype=time_type), (B, 2)) if np.ndim(tspan) == 1 else np.asarray(tspan)
+    probs = DeviceProblems(f, u0, p, tsp, time_type, dev)
+    r = _solve_device(probs, alg, True, dt=dt, abstol=abstol, reltol=reltol, trace=True, driver=driver)
+    rt = _solve_device(probs, alg, True, dt=dt, abstol=abstol / tighten, reltol=reltol / tighten, driver=driver)
+    u = r.us[:, 1].double()
+    ut = rt.us[:, 1].double()
+    err = ((u - ut).norm(dim=1) / ut.norm(dim=1).clamp_min(1e-3)).cpu().numpy()
+    work = (r.naccept + r.nreject).cpu().numpy()
+    return r.dt_first.cpu().numpy(), err, work
+
+
+def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_quantile=0.9, safety=0.5,
+                   epochs=8, seed=0, log=None):
+    """Train a StepSizeModel on the plain solver's traces of the given ensemble.
+
+    The common error target is `safety` times the `target_quantile` of the plain run's
+    final-state error proxy, so the learned run aims at the plain run's error level."""
+    dtf, err, _ = solver_traces(f, u0, p, tspan, time_type, alg, reltol=reltol, abstol=abstol)
+    target = safety * float(np.quantile(err[np.isfinite(err)], target_quantile))
+    y, w = training_targets(dtf, err, target, alpha=1.0)
+    x = features(u0, p, np.full(u0.shape[0], reltol))
+    m = StepSizeModel(x.shape[1], seed=seed)
+    m.fit(x, y, w, epochs=epochs, seed=seed, log=log)
+    return m, {"target_err": target, "err_proxy_median": float(np.median(err)), "n_train": int(u0.shape[0])}

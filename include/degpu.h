@@ -107,6 +107,7 @@ typedef struct degpu_outputs {
   signed char* retcode; /* optional [B] */
   int* naccept;         /* optional [B] */
   int* nreject;         /* optional [B] */
+  float* dt_first;      /* optional [B]: first accepted step size (accepted-step trace) */
 } degpu_outputs;
 
 const char* degpu_version(void);
