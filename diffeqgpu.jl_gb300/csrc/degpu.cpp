@@ -246,7 +246,16 @@ const char* kernel_name(int driver) {
 int ensure_context() {
   int rc = load_driver();
   if (rc) return rc;
-  CUDA_TRY(cudaFree(0));  // makes the runtime's primary context of the current device current
+  // make the runtime's primary context of the current device current -- once per device,
+  // so that later solves (possibly inside a stream capture) issue no context calls
+  static std::mutex mu;
+  static unsigned long long done = 0;
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 64 && (done >> dev) & 1ULL) return 0;
+  CUDA_TRY(cudaFree(0));
+  if (dev < 64) done |= 1ULL << dev;
   return 0;
 }
 
@@ -594,6 +603,28 @@ int degpu_kernel_info(const degpu_rhs* f, const degpu_options* opt, int adaptive
   if (local_bytes) *local_bytes = K.local_bytes;
   if (max_threads) *max_threads = K.max_threads;
   return 0;
+}
+
+int degpu_learned_asolve(const degpu_rhs* f, const degpu_mlp* m, const degpu_problems* probs, const degpu_options* opt,
+                         float dt_lo, float dt_hi, float s_max, degpu_outputs* out, void* stream) {
+  if (!f || !m || !probs || !opt || !out) return fail(DEGPU_E_INVALID, "null argument");
+  if (probs->B < 0) return fail(DEGPU_E_INVALID, "negative trajectory count");
+  if (probs->B == 0) return 0;
+  if (!(s_max >= 1.0f) || !(dt_lo > 0.0f) || !(dt_hi >= dt_lo)) return fail(DEGPU_E_INVALID, "bad dt / scale clamp");
+  cudaStream_t s = (cudaStream_t)stream;
+  float* scratch = nullptr;  // dt0 [B] followed by tolscale [B]
+  CUDA_TRY(cudaMallocAsync((void**)&scratch, sizeof(float) * 2 * (size_t)probs->B, s));
+  int rc = degpu_mlp_infer_problems(m, probs->u0, f->N, probs->p, f->P, (float)opt->reltol, probs->B, scratch,
+                                    scratch + probs->B, dt_lo, dt_hi, 1.0f, s_max, stream);
+  if (rc) rc = fail(rc, "step-size model inference failed (does the model's input width match N + P + 1?)");
+  if (!rc) {
+    degpu_options o = *opt;
+    o.dt0 = scratch;
+    o.tolscale = scratch + probs->B;
+    rc = degpu_vectorized_asolve(f, probs, &o, out, stream);
+  }
+  cudaFreeAsync(scratch, s);
+  return rc;
 }
 
 // ------------------------------------------------------------------ autotuner

@@ -860,6 +860,11 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, long long i) {
     if (++L.nattempt > P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
     attempt<true>(L, t, dt, unew, err);
     float EEst = scaled_norm(err, L.uprev, unew, L.abstol, L.reltol);
+#if !DEGPU_PARITY
+    // fast mode: a NaN error estimate ends the trajectory at once (the reference accepts
+    // the step and lets the NaN run to the end of the span; the outcome is Unstable either way)
+    if (EEst != EEst) { L.status = DEGPU_RET_UNSTABLE; return true; }
+#endif
     if (!controller(L, EEst, dt, t)) {
       L.dtnew = dt;
       L.nreject++;

@@ -66,8 +66,18 @@ struct InferSmem {
   float mean[KIN], rstd[KIN];
 };
 
+// Features come either from x [B][n_in] or, when x is null, straight from the problem batch:
+// (u0 [B][Nu], p [B][Np], logtol), n_in = Nu + Np + 1.
+struct FeatSrc {
+  const float* x;
+  const float* u0;
+  const float* p;
+  int Nu, Np;
+  float logtol;
+};
+
 __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* __restrict__ P, int n_in, const float* __restrict__ mean,
-                                                        const float* __restrict__ stdv, const float* __restrict__ x, long long B,
+                                                        const float* __restrict__ stdv, const FeatSrc src, long long B,
                                                         float* __restrict__ y, float* __restrict__ dt0, float* __restrict__ tsc,
                                                         float dt_lo, float dt_hi, float s_lo, float s_hi) {
   __shared__ InferSmem S;
@@ -95,7 +105,12 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* __restrict_
     const long long r0 = tile * 16 + g, r1 = r0 + 8;
     auto feat = [&](long long r, int k) -> float {
       if (r >= B || k >= n_in) return 0.0f;
-      return (x[r * n_in + k] - S.mean[k]) * S.rstd[k];
+      float v;
+      if (src.x) v = src.x[r * n_in + k];
+      else if (k < src.Nu) v = src.u0[r * src.Nu + k];
+      else if (k < src.Nu + src.Np) v = src.p[r * src.Np + (k - src.Nu)];
+      else v = src.logtol;
+      return (v - S.mean[k]) * S.rstd[k];
     };
     uint32_t a[4];
     a[0] = pack_bf16(feat(r0, tig * 2), feat(r0, tig * 2 + 1));
@@ -388,8 +403,26 @@ int degpu_mlp_infer(const degpu_mlp* m, const float* x, long long B, float* y, f
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   long long tiles = (B + 15) / 16;
   long long grid = std::min<long long>((tiles + 3) / 4, (long long)sms * 8);
-  mlp_infer_kernel<<<(int)grid, 128, 0, (cudaStream_t)stream>>>(m->P, m->n_in, m->mean, m->stdv, x, B, y, dt0, tolscale,
+  FeatSrc src{x, nullptr, nullptr, 0, 0, 0.0f};
+  mlp_infer_kernel<<<(int)grid, 128, 0, (cudaStream_t)stream>>>(m->P, m->n_in, m->mean, m->stdv, src, B, y, dt0, tolscale,
                                                                  dt_lo, dt_hi, s_lo, s_hi);
+  return cudaGetLastError() == cudaSuccess ? 0 : DEGPU_E_CUDA;
+}
+
+int degpu_mlp_infer_problems(const degpu_mlp* m, const float* u0, int n_state, const float* p, int n_param, float reltol,
+                             long long B, float* dt0, float* tolscale, float dt_lo, float dt_hi, float s_lo, float s_hi,
+                             void* stream) {
+  if (!m || B < 0 || n_state + n_param + 1 != m->n_in || !(reltol > 0.0f)) return DEGPU_E_INVALID;
+  if (B == 0) return 0;
+  if (!u0 || (n_param > 0 && !p)) return DEGPU_E_INVALID;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long tiles = (B + 15) / 16;
+  long long grid = std::min<long long>((tiles + 3) / 4, (long long)sms * 8);
+  FeatSrc src{nullptr, u0, p, n_state, n_param, log10f(reltol)};
+  mlp_infer_kernel<<<(int)grid, 128, 0, (cudaStream_t)stream>>>(m->P, m->n_in, m->mean, m->stdv, src, B, nullptr, dt0,
+                                                                 tolscale, dt_lo, dt_hi, s_lo, s_hi);
   return cudaGetLastError() == cudaSuccess ? 0 : DEGPU_E_CUDA;
 }
 

@@ -160,9 +160,13 @@ def training_targets(first_dt, err, target_err, *, alpha=1.0, s_max=1e3, err_flo
     return y, w
 
 
-def solver_traces(f, u0, p, tspan, time_type, alg, *, reltol, abstol, dt=0.1, tighten=32.0, device=None, driver="persistent"):
-    """Run the plain solver twice (at the given tolerances and `tighten` x tighter) and return
-    (first accepted dt, final-state error proxy, naccept + nreject) per trajectory."""
+def solver_traces(f, u0, p, tspan, time_type, alg, *, reltol, abstol, dt=0.1, scales=(1, 2, 4, 8, 16, 32, 64),
+                  tighten=64.0, device=None, driver="persistent"):
+    """Accepted-step traces of the plain solver on a training ensemble (all on the GPU).
+
+    Returns the first accepted dt at the base tolerances, the final-state error proxy at
+    each tolerance scale s (distance to a `tighten` x tighter plain solve, relative to its
+    norm) as an array [len(scales), B], and the attempts per trajectory at s = 1."""
     import torch
 
     from .api import DeviceProblems, _solve_device
@@ -170,25 +174,48 @@ def solver_traces(f, u0, p, tspan, time_type, alg, *, reltol, abstol, dt=0.1, ti
     B = u0.shape[0]
     tsp = np.broadcast_to(np.asarray(tspan, dtype=time_type), (B, 2)) if np.ndim(tspan) == 1 else np.asarray(tspan)
     probs = DeviceProblems(f, u0, p, tsp, time_type, dev)
-    r = _solve_device(probs, alg, True, dt=dt, abstol=abstol, reltol=reltol, trace=True, driver=driver)
-    rt = _solve_device(probs, alg, True, dt=dt, abstol=abstol / tighten, reltol=reltol / tighten, driver=driver)
-    u = r.us[:, 1].double()
-    ut = rt.us[:, 1].double()
-    err = ((u - ut).norm(dim=1) / ut.norm(dim=1).clamp_min(1e-3)).cpu().numpy()
-    work = (r.naccept + r.nreject).cpu().numpy()
-    return r.dt_first.cpu().numpy(), err, work
+    ref = _solve_device(probs, alg, True, dt=dt, abstol=abstol / tighten, reltol=reltol / tighten, driver=driver)
+    ur = ref.us[:, 1].double()
+    nr = ur.norm(dim=1).clamp_min(1e-3)
+    errs, dtf, work = [], None, None
+    for s in scales:
+        r = _solve_device(probs, alg, True, dt=dt, abstol=abstol * s, reltol=reltol * s, trace=(s == scales[0]),
+                          driver=driver)
+        e = ((r.us[:, 1].double() - ur).norm(dim=1) / nr)
+        e = torch.where(r.retcode == 1, e, torch.full_like(e, float("inf")))
+        errs.append(e.cpu().numpy())
+        if s == scales[0]:
+            dtf = r.dt_first.cpu().numpy()
+            work = (r.naccept + r.nreject).cpu().numpy()
+    return dtf, np.stack(errs), work
+
+
+def scale_targets(errs, scales, target_err):
+    """Largest measured tolerance scale whose error, and that of every smaller scale, stays
+    at or below the target (1 if even the base tolerance misses it)."""
+    ok = np.cumprod(errs <= target_err, axis=0).astype(bool)  # monotone prefix
+    idx = ok.sum(axis=0) - 1
+    sc = np.asarray(scales, np.float64)
+    return np.where(idx >= 0, sc[np.clip(idx, 0, len(sc) - 1)], sc[0])
 
 
 def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_quantile=0.9, safety=0.5,
-                   epochs=8, seed=0, log=None):
+                   scales=(1, 2, 4, 8, 16, 32, 64), epochs=8, seed=0, log=None):
     """Train a StepSizeModel on the plain solver's traces of the given ensemble.
 
     The common error target is `safety` times the `target_quantile` of the plain run's
-    final-state error proxy, so the learned run aims at the plain run's error level."""
-    dtf, err, _ = solver_traces(f, u0, p, tspan, time_type, alg, reltol=reltol, abstol=abstol)
-    target = safety * float(np.quantile(err[np.isfinite(err)], target_quantile))
-    y, w = training_targets(dtf, err, target, alpha=1.0)
+    error proxy at the base tolerances; each trajectory's scale target is the largest
+    tolerance scale at which its measured error proxy stays under that target."""
+    dtf, errs, _ = solver_traces(f, u0, p, tspan, time_type, alg, reltol=reltol, abstol=abstol, scales=scales)
+    e1 = errs[0][np.isfinite(errs[0])]
+    target = safety * float(np.quantile(e1, target_quantile))
+    s = scale_targets(errs, scales, target)
+    ok = np.isfinite(dtf) & (dtf > 0)
+    y = np.stack([np.log(np.where(ok, dtf, 1.0)), np.log(s)], 1).astype(np.float32)
+    w = np.stack([ok, np.ones_like(ok)], 1).astype(np.float32)
     x = features(u0, p, np.full(u0.shape[0], reltol))
     m = StepSizeModel(x.shape[1], seed=seed)
+    m.scale_range = (1.0, float(max(scales)))
     m.fit(x, y, w, epochs=epochs, seed=seed, log=log)
-    return m, {"target_err": target, "err_proxy_median": float(np.median(err)), "n_train": int(u0.shape[0])}
+    return m, {"target_err": target, "err_proxy_median": float(np.median(e1)), "n_train": int(u0.shape[0]),
+               "scale_target_median": float(np.median(s)), "scale_target_mean_log": float(np.log(s).mean())}

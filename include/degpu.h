@@ -196,6 +196,17 @@ int degpu_mlp_get_params(const degpu_mlp* m, float* host_params, float* host_gra
  * clamp(exp(y1), s_lo, s_hi) (each optional). */
 int degpu_mlp_infer(const degpu_mlp* m, const float* x, long long B, float* y, float* dt0, float* tolscale,
                     float dt_lo, float dt_hi, float s_lo, float s_hi, void* stream);
+/* Same, with the features read straight from a problem batch: x = (u0 [B][n_state],
+ * p [B][n_param], log10 reltol); requires n_in == n_state + n_param + 1. */
+int degpu_mlp_infer_problems(const degpu_mlp* m, const float* u0, int n_state, const float* p, int n_param, float reltol,
+                             long long B, float* dt0, float* tolscale, float dt_lo, float dt_hi, float s_lo, float s_hi,
+                             void* stream);
+/* Learned-controller adaptive solve: degpu_mlp_infer_problems into per-trajectory dt0 and
+ * tolerance-scale arrays (8 bytes per trajectory of scratch, from the stream-ordered
+ * allocator), then degpu_vectorized_asolve with them.  opt->dt0 / opt->tolscale are
+ * ignored; dt0 is clamped to [dt_lo, dt_hi], the scale to [1, s_max]. */
+int degpu_learned_asolve(const degpu_rhs* f, const degpu_mlp* m, const degpu_problems* probs, const degpu_options* opt,
+                         float dt_lo, float dt_hi, float s_max, degpu_outputs* out, void* stream);
 /* Gradient of the weighted mean squared error over a device batch (target, weight [B][2];
  * weight may be NULL) into the model's gradient buffer; *loss (device scalar, optional). */
 int degpu_mlp_grad(degpu_mlp* m, const float* x, const float* target, const float* weight, long long B, float* loss,
