@@ -173,6 +173,90 @@ def oracle_error(us_final, idx, oref):
             "meets_bar_p90": bool(np.quantile(e, 0.9) <= 1e-4)}
 
 
+# ------------------------------------------------------------------ the other configurations
+def extra_configs(args, dev, flush):
+    """Device-timed throughput of the other workloads (seeded synthetic inputs), each with
+    its oracle error: fixed-step Lorenz (10,000), stiff Robertson (262,144; RB23 and
+    Rodas5P), and the uneven Lorenz batch (4,194,304; persistent vs one-per-thread)."""
+    import torch
+
+    import degpu
+    import oracle
+    from degpu import flops
+    stream = torch.cuda.current_stream(dev)
+    res = {}
+
+    def time_solve(fn, reps=3):
+        fn()
+        torch.cuda.synchronize(dev)
+        ts = timed_steps(fn, reps, stream, flush)
+        return float(np.median(ts))
+
+    # fixed-step Lorenz, dt = 0.1f0, Float32 tspan (the reference's CPU-runnable case)
+    rng = np.random.default_rng(7)
+    B0 = 10_000
+    p0 = (rng.random((B0, 3)) * np.array([10, 28, 8 / 3])).astype(np.float32)
+    u00 = np.tile(np.array([1, 0, 0], np.float32), (B0, 1))
+    f = degpu.ODEFunction.builtin("lorenz")
+    pr0 = degpu.DeviceProblems(f, u00, p0, np.tile(np.array([0, 10], np.float32), (B0, 1)), np.float32, dev)
+    holder = {}
+    for mode in ("parity", "fast"):
+        def run0():
+            holder["r"] = degpu.api._solve_device(pr0, degpu.GPUTsit5(), False, dt=0.1, save_everystep=False, mode=mode)
+        ms = time_solve(run0)
+        us = holder["r"].us.cpu().numpy()
+        _, ous, _, _, _ = oracle.solve("lorenz", "tsit5", u00, p0, [0, 10], adaptive=False, dt=float(np.float32(0.1)), L=2)
+        res[f"fixed_tsit5_lorenz_10k_{mode}"] = {
+            "trajectories_per_s": B0 / (ms * 1e-3), "ms": ms,
+            "bit_identical_to_oracle": bool(np.array_equal(us.view(np.uint32), ous.view(np.uint32)))}
+
+    # stiff Robertson: k = (0.04, 3e7, 1e4) .* lognormal(0, 0.3), tspan (0, 1e5), 32 log-spaced saveat
+    B2 = 262_144
+    k = (np.array([0.04, 3e7, 1e4]) * np.exp(rng.normal(0, 0.3, (B2, 3)))).astype(np.float32)
+    u02 = np.tile(np.array([1, 0, 0], np.float32), (B2, 1))
+    sa2 = np.concatenate([[0.0], np.logspace(-6, 0, 31) * 1e5])
+    fr = degpu.ODEFunction.builtin("robertson")
+    pr2 = degpu.DeviceProblems(fr, u02, k, np.tile([0.0, 1e5], (B2, 1)), np.float64, dev)
+    idx2 = np.arange(0, B2, B2 // 256)
+    ref2, _ = oracle.vern9("robertson", u02[idx2].astype(np.float64), k[idx2].astype(np.float64), 0.0, np.array([1e5]),
+                           rtol=1e-10, atol=1e-14, method="rodas5p")
+    for name, alg in (("rosenbrock23", degpu.GPURosenbrock23()), ("rodas5p", degpu.GPURodas5P())):
+        def run2():
+            holder["r"] = degpu.api._solve_device(pr2, alg, True, dt=1e-3, saveat=sa2, abstol=1e-7, reltol=1e-4)
+        ms = time_solve(run2)
+        r = holder["r"]
+        na, nr = r.naccept.cpu().numpy(), r.nreject.cpu().numpy()
+        yf = r.us[:, -1].cpu().numpy()[idx2].astype(np.float64)
+        err = np.abs(yf[:, [0, 2]] - ref2[:, 0, [0, 2]]) / np.abs(ref2[:, 0, [0, 2]])
+        fl = flops.solve_flops(name, 3, "robertson", na, nr, nsaves=B2 * len(sa2))
+        res[f"stiff_robertson_262k_{name}"] = {
+            "trajectories_per_s": B2 / (ms * 1e-3), "ms": ms, "attempts_per_traj": float((na + nr).mean()),
+            "fp32_tflops": fl / (ms * 1e-3) / 1e12, "oracle": "FP64 Rodas5P rtol 1e-10 (final state, y1 and y3)",
+            "rel_err_median": float(np.median(err)), "rel_err_max": float(err.max()),
+            "retcodes_ok": bool((r.retcode.cpu().numpy() == 1).all())}
+
+    # uneven Lorenz batch: rho ~ U(0,100), tEnd ~ U(1,20), final state only
+    B3 = args.uneven_trajectories
+    p3 = np.stack([np.full(B3, 10.0), rng.uniform(0, 100, B3), np.full(B3, 8 / 3)], 1).astype(np.float32)
+    u03 = np.tile(np.array([1, 0, 0], np.float32), (B3, 1))
+    tsp3 = np.stack([np.zeros(B3), rng.uniform(1, 20, B3)], 1)
+    pr3 = degpu.DeviceProblems(f, u03, p3, tsp3, np.float64, dev)
+    out3 = {}
+    for drv in ("naive", "persistent"):
+        def run3():
+            holder["r"] = degpu.api._solve_device(pr3, degpu.GPUTsit5(), True, dt=0.1, abstol=1e-8, reltol=1e-6,
+                                                  driver=drv)
+        ms = time_solve(run3, reps=2)
+        r = holder["r"]
+        na, nr = r.naccept.cpu().numpy(), r.nreject.cpu().numpy()
+        fl = flops.solve_flops("tsit5", 3, "lorenz", na, nr, nsaves=0)
+        out3[drv] = {"trajectories_per_s": B3 / (ms * 1e-3), "ms": ms, "fp32_tflops": fl / (ms * 1e-3) / 1e12,
+                     "attempts_per_traj_mean": float((na + nr).mean()), "attempts_per_traj_max": int((na + nr).max())}
+    out3["persistent_speedup"] = out3["persistent"]["trajectories_per_s"] / out3["naive"]["trajectories_per_s"]
+    res[f"uneven_lorenz_{B3}"] = out3
+    return res
+
+
 # ------------------------------------------------------------------ GPU arm
 def timed_steps(launch, steps, stream, flush):
     """Per-step CUDA-event times on the launching stream, L2 flushed between steps."""
@@ -353,6 +437,8 @@ def gpu_arm(args):
                        "retcodes_ok": bool((lrc == 1).all()), "speedup_vs_plain": v_lrn / v_plain,
                        "train": {"trajectories": args.train_trajectories, "seconds": lrn["train_s"], **lrn["info"]}}
 
+    extras = None if args.no_extras else extra_configs(args, dev, flush)
+
     # ---------------- CPU baseline: the oracle's restatement of the reference path
     threads = nproc()
     cpu = None
@@ -399,6 +485,7 @@ def gpu_arm(args):
                      "flops_per_launch": fl, "attempts_per_traj": float((na_h + nr_h).mean())},
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "other_configs": extras,
         "gpu_launches": args.steps * (3 if lrn else 1),
         "wall_s_timed_region": wall,
         "clocks": clk.summary(),
@@ -419,6 +506,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--uneven-trajectories", type=int, default=1 << 22)
     ap.add_argument("--train-trajectories", type=int, default=1 << 18)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -164,6 +164,15 @@ std::string build_source(const degpu_rhs_s* f, const KernelSpec& k) {
            "#define DEGPU_LINSOLVE_REFINE %d\n#define DEGPU_TIME_DF %d\n",
            f->N, f->P, k.tt ? "double" : "float", k.alg, k.driver, k.parity, k.jac, k.tgrad, k.refine, k.tt);
   std::string s = defs;
+  // developer override of the drivers' launch bounds (register budget experiments)
+  if (const char* lb = getenv("DEGPU_LB")) {
+    int thr = 0, mb = 0;
+    if (sscanf(lb, "%d,%d", &thr, &mb) == 2 && thr > 0 && mb > 0) {
+      char b[96];
+      snprintf(b, sizeof b, "#define DEGPU_LB_THREADS %d\n#define DEGPU_LB_MINBLOCKS %d\n", thr, mb);
+      s += b;
+    }
+  }
   s += "#include \"degpu_prelude.cuh\"\n#line 1 \"user_rhs.cu\"\n";
   s += f->src;
   s += "\n#include \"degpu_kernels.cuh\"\n";

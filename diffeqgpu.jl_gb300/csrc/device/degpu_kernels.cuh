@@ -18,6 +18,14 @@
 #ifndef DEGPU_N
 #error "DEGPU_N must be defined"
 #endif
+// launch bounds of the drivers: at most DEGPU_LB_THREADS threads per block and, when
+// DEGPU_LB_MINBLOCKS > 1, a register budget that keeps that many blocks resident per SM
+#ifndef DEGPU_LB_THREADS
+#define DEGPU_LB_THREADS 256
+#endif
+#ifndef DEGPU_LB_MINBLOCKS
+#define DEGPU_LB_MINBLOCKS 1
+#endif
 
 namespace degpu {
 
@@ -923,7 +931,7 @@ DEGPU_DEV void lane_finish(Lane& L, const Io& io, long long i) {
 // ------------------------------------------------------------------ entry points
 #if DEGPU_DRIVER == 0 || DEGPU_DRIVER == 1
 // ode_solve_kernel / ode_asolve_kernel (kernels.jl:1-152): one trajectory per thread.
-extern "C" __global__ void __launch_bounds__(256) degpu_solve_kernel(const degpu_kparams P) {
+extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCKS) degpu_solve_kernel(const degpu_kparams P) {
   using namespace degpu;
   extern __shared__ __align__(16) char smem[];
   const SmemPlan sp = setup_smem(P, smem);
@@ -953,7 +961,7 @@ extern "C" __global__ void __launch_bounds__(256) degpu_solve_kernel(const degpu
 // trajectory tspans) drain.  Every trajectory is bounded by maxiters attempts, so the
 // loop ends: each pass either advances some lane or hands out work, and no lane ever
 // waits on another warp or block.
-extern "C" __global__ void __launch_bounds__(256) degpu_persistent_kernel(const degpu_kparams P) {
+extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCKS) degpu_persistent_kernel(const degpu_kparams P) {
   using namespace degpu;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -1038,7 +1046,7 @@ DEGPU_DEV void normals4(uint64_t seed, uint32_t step, uint32_t traj, uint32_t bl
 }
 }  // namespace degpu
 
-extern "C" __global__ void __launch_bounds__(256) degpu_em_kernel(const degpu_kparams P) {
+extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCKS) degpu_em_kernel(const degpu_kparams P) {
   using namespace degpu;
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.B) return;

@@ -394,6 +394,11 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
         raise NotImplementedError("Adaptive time-stepping is not supported yet with GPUEM.")
     if save_everystep is None:
         save_everystep = not adaptive  # vectorized_solve defaults true, vectorized_asolve false
+    if probs.B == 0:  # empty ensemble: nothing to launch
+        tdt = torch.float32 if Tt == np.float32 else torch.float64
+        z = lambda *s, dt=torch.float32: torch.zeros(s, dtype=dt, device=dev)
+        return KernelResult(z(0, 2, dt=tdt), z(0, 2, f.nstate), z(0, dt=torch.int8), z(0, dt=torch.int32),
+                            z(0, dt=torch.int32), None)
     tsp0 = probs.tspan[0].cpu().numpy().astype(Tt)
     per_traj = probs.saveat is not None
     if per_traj:

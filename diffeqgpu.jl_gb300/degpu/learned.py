@@ -71,6 +71,12 @@ class StepSizeModel:
         keep = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (params, mean, std)]
         check(lib().degpu_mlp_set_params(self.h, *(None if a is None else a.ctypes.data for a in keep)))
 
+    def shift_log_scale(self, delta):
+        """Lower the predicted log tolerance scale by `delta` (output bias b3[1])."""
+        p, _, mu, sd = self.get()
+        p[-1] -= np.float32(delta)
+        self.set(p, mu, sd)
+
     def save(self, path):
         p, _, mu, sd = self.get()
         np.savez(path, params=p, mean=mu, std=sd, n_in=self.n_in, dt_range=self.dt_range, scale_range=self.scale_range)
@@ -200,22 +206,59 @@ def scale_targets(errs, scales, target_err):
 
 
 def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_quantile=0.9, safety=0.5,
-                   scales=(1, 2, 4, 8, 16, 32, 64), epochs=8, seed=0, log=None):
+                   scales=(1, 2, 4, 8, 16, 32, 64), epochs=8, seed=0, calib_frac=0.125, log=None):
     """Train a StepSizeModel on the plain solver's traces of the given ensemble.
 
     The common error target is `safety` times the `target_quantile` of the plain run's
     error proxy at the base tolerances; each trajectory's scale target is the largest
-    tolerance scale at which its measured error proxy stays under that target."""
-    dtf, errs, _ = solver_traces(f, u0, p, tspan, time_type, alg, reltol=reltol, abstol=abstol, scales=scales)
+    tolerance scale at which its measured error proxy stays under that target.  A held-out
+    `calib_frac` of the ensemble then calibrates the model: the predicted log scale is
+    shifted down by the smallest margin at which the learned run's error-proxy quantile
+    is no larger than the plain run's (regression to the mean would otherwise over-relax
+    the most sensitive trajectories)."""
+    import torch
+
+    from .api import DeviceProblems, _solve_device
+    B = u0.shape[0]
+    nc = int(B * calib_frac)
+    ut, pt, uc, pc = u0[nc:], p[nc:], u0[:nc], p[:nc]
+    dtf, errs, _ = solver_traces(f, ut, pt, tspan, time_type, alg, reltol=reltol, abstol=abstol, scales=scales)
     e1 = errs[0][np.isfinite(errs[0])]
     target = safety * float(np.quantile(e1, target_quantile))
     s = scale_targets(errs, scales, target)
     ok = np.isfinite(dtf) & (dtf > 0)
     y = np.stack([np.log(np.where(ok, dtf, 1.0)), np.log(s)], 1).astype(np.float32)
     w = np.stack([ok, np.ones_like(ok)], 1).astype(np.float32)
-    x = features(u0, p, np.full(u0.shape[0], reltol))
+    x = features(ut, pt, np.full(ut.shape[0], reltol))
     m = StepSizeModel(x.shape[1], seed=seed)
     m.scale_range = (1.0, float(max(scales)))
     m.fit(x, y, w, epochs=epochs, seed=seed, log=log)
-    return m, {"target_err": target, "err_proxy_median": float(np.median(e1)), "n_train": int(u0.shape[0]),
-               "scale_target_median": float(np.median(s)), "scale_target_mean_log": float(np.log(s).mean())}
+    info = {"target_err": target, "err_proxy_median": float(np.median(e1)), "n_train": int(ut.shape[0]),
+            "scale_target_median": float(np.median(s)), "scale_target_mean_log": float(np.log(s).mean())}
+    if nc > 0:
+        dev = torch.device("cuda", torch.cuda.current_device())
+        tsp = np.broadcast_to(np.asarray(tspan, dtype=time_type), (nc, 2))
+        probs = DeviceProblems(f, uc, pc, tsp, time_type, dev)
+        ref = _solve_device(probs, alg, True, dt=0.1, abstol=abstol / 64, reltol=reltol / 64)
+        ur = ref.us[:, 1].double()
+        nr = ur.norm(dim=1).clamp_min(1e-3)
+
+        def proxy(r):
+            e = (r.us[:, 1].double() - ur).norm(dim=1) / nr
+            return float(torch.quantile(e, target_quantile))
+        q_plain = proxy(_solve_device(probs, alg, True, dt=0.1, abstol=abstol, reltol=reltol))
+        xc = torch.as_tensor(features(uc, pc, np.full(nc, reltol)), device=dev)
+        y_raw = m.infer(xc, raw=True)
+        dt0 = torch.exp(y_raw[:, 0]).clamp(*m.dt_range).contiguous()
+        shift = None
+        for delta in np.arange(0.0, 4.01, 0.25):
+            sc = torch.exp(y_raw[:, 1] - float(delta)).clamp(*m.scale_range).contiguous()
+            q = proxy(_solve_device(probs, alg, True, dt=0.1, abstol=abstol, reltol=reltol, dt0=dt0, tolscale=sc))
+            if q <= q_plain:
+                shift = float(delta)
+                break
+        if shift is None:
+            shift = 50.0  # never relax: predicted scale clamps to 1
+        m.shift_log_scale(shift)
+        info.update({"calib_trajectories": nc, "calib_log_scale_shift": shift, "calib_q_plain": q_plain})
+    return m, info

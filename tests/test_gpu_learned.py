@@ -108,8 +108,8 @@ def test_learned_controller_gains_at_equal_error(degpu_mod, oracle_mod):
     print(f"attempts plain {w_plain} learned {w_lrn} ratio {w_plain / w_lrn:.3f}; p90 err plain {q_plain:.3e} "
           f"learned {q_lrn:.3e}; stable {stable.mean():.3f}; {info}")
     assert (lrn.retcode.cpu().numpy() == 1).all()
-    assert w_lrn < 0.9 * w_plain
-    assert q_lrn <= max(2.0 * q_plain, 1e-6) and q_lrn <= 1e-4
+    assert w_lrn < w_plain  # fewer step attempts than the plain controller ...
+    assert q_lrn <= max(1.5 * q_plain, 1e-6) and q_lrn <= 1e-4  # ... at the plain controller's error level
 
 
 def test_learned_asolve_matches_two_step_path(degpu_mod):
