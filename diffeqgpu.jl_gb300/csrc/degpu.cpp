@@ -26,6 +26,7 @@
 #include <unistd.h>
 #include <vector>
 
+#include "degpu_internal.h"
 #include "device/degpu_params.h"
 
 // embedded device sources (generated by build.py from csrc/device and csrc/models)
@@ -772,3 +773,35 @@ void degpu_plan_destroy(degpu_plan* plan) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ internal helpers
+int degpu_internal_rhs_dims(const degpu_rhs* f, int* n_state, int* n_param) {
+  if (!f) return fail(DEGPU_E_INVALID, "null right-hand side");
+  if (n_state) *n_state = f->N;
+  if (n_param) *n_param = f->P;
+  return 0;
+}
+
+int degpu_internal_fail(int code, const char* msg) { return fail(code, msg ? msg : ""); }
+
+int degpu_internal_asolve_with_work(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
+                                    degpu_outputs* out, unsigned long long* work, void* stream) {
+  Request rq;
+  int rc = make_request(f, probs, opt, 1, out, &rq);
+  if (rc) return rc;
+  if (rq.kp.B == 0) return 0;
+  Kernel K;
+  rc = get_kernel(f, rq.spec, &K);
+  if (rc) return rc;
+  int block = rq.block ? rq.block : default_block(rq);
+  int chunk = rq.chunk ? rq.chunk : default_chunk();
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    char key[64];
+    snprintf(key, sizeof key, "%p|%lld", (void*)K.fn, (long long)(rq.kp.B >> 16));
+    auto it = g_tuned.find(key);
+    if (!rq.block && it != g_tuned.end()) { block = it->second.first; if (!rq.chunk) chunk = it->second.second; }
+  }
+  if (rq.spec.driver == 2 && !work) return fail(DEGPU_E_INVALID, "persistent driver needs a work counter");
+  return launch(rq, K, block, chunk, work, (CUstream)stream);
+}

@@ -83,6 +83,9 @@ SIGNATURES = {
                                                 ctypes.c_float, ctypes.c_float, _P]),
     "degpu_learned_asolve": (ctypes.c_int, [_P, _P, ctypes.POINTER(Problems), ctypes.POINTER(Options), ctypes.c_float,
                                             ctypes.c_float, ctypes.c_float, ctypes.POINTER(Outputs), _P]),
+    "degpu_learned_asolve_noalloc": (ctypes.c_int, [_P, _P, ctypes.POINTER(Problems), ctypes.POINTER(Options),
+                                                    ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                                    ctypes.POINTER(Outputs), _P]),
     "degpu_mlp_grad": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_longlong, _P, _P]),
     "degpu_mlp_adam_step": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                            ctypes.c_float, _P]),

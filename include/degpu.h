@@ -207,6 +207,21 @@ int degpu_mlp_infer_problems(const degpu_mlp* m, const float* u0, int n_state, c
  * ignored; dt0 is clamped to [dt_lo, dt_hi], the scale to [1, s_max]. */
 int degpu_learned_asolve(const degpu_rhs* f, const degpu_mlp* m, const degpu_problems* probs, const degpu_options* opt,
                          float dt_lo, float dt_hi, float s_max, degpu_outputs* out, void* stream);
+/* degpu_learned_asolve for callers that cannot allocate device memory during a solve
+ * (host callbacks, fixed-budget or real-time runtimes that own all device memory).  No
+ * counterpart in the reference.  Same arguments and results as degpu_learned_asolve, but
+ * its scratch (dt0 and tolerance scale, 8 bytes per trajectory, plus the work counter)
+ * is a static array in the library's device image sized for at most
+ * DEGPU_NOALLOC_MAX_TRAJECTORIES trajectories per call (larger calls return
+ * DEGPU_E_INVALID).  It calls no allocator.  The first call on a device resolves the
+ * array's address (cudaGetSymbolAddress), and the first call with a new right-hand side or
+ * option set compiles and loads its kernels: make those first calls before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
+#define DEGPU_NOALLOC_MAX_TRAJECTORIES 262144
+int degpu_learned_asolve_noalloc(const degpu_rhs* f, const degpu_mlp* m, const degpu_problems* probs,
+                                 const degpu_options* opt, float dt_lo, float dt_hi, float s_max, degpu_outputs* out,
+                                 void* stream);
 /* Gradient of the weighted mean squared error over a device batch (target, weight [B][2];
  * weight may be NULL) into the model's gradient buffer; *loss (device scalar, optional). */
 int degpu_mlp_grad(degpu_mlp* m, const float* x, const float* target, const float* weight, long long B, float* loss,
