@@ -461,7 +461,7 @@ def gpu_arm(args):
     # headline: the learned controller when it holds the plain run's error level and the bar
     use_learned = bool(learned_rec and learned_rec["retcodes_ok"]
                        and learned_rec["oracle_error"]["p90"] <= max(err_plain["p90"] * 1.25, 0.0)
-                       and learned_rec["oracle_error"]["p90"] <= 1e-4)
+                       and learned_rec["oracle_error"]["p90"] <= 1e-4 and v_lrn > v_plain)
     value = v_lrn if use_learned else v_plain
     line = {
         "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
