@@ -448,15 +448,12 @@ def gpu_arm(args):
         cpu = {"value": rate, "unit": "trajectories/s", "cores": threads, "kind": "port",
                "sample": f"first {sample} of the {B} trajectories, same workload, OpenMP over trajectories"}
 
-    traffic = None
-    prof = ROOT / "profiles" / "traffic.json"
-    if prof.exists():
-        try:
-            tj = json.loads(prof.read_text())
-            per = tj.get("persistent_tsit5_lorenz_bytes_per_traj")
-            traffic = None if per is None else per * B
-        except Exception:
-            traffic = None
+    # DRAM bytes per trajectory of the persistent kernel on this workload, from one ncu
+    # capture (dram__bytes_read.sum + dram__bytes_write.sum of a 524,288-trajectory launch,
+    # profiles/persistent_tsit5_lorenz_staged.md) scaled by the trajectories of one launch:
+    # the kernel streams each trajectory's inputs once and writes its output columns once,
+    # so its traffic grows in proportion to B.
+    traffic = TRAFFIC_BYTES_PER_TRAJ * B
 
     # headline: the learned controller when it holds the plain run's error level and the bar
     use_learned = bool(learned_rec and learned_rec["retcodes_ok"]
@@ -494,6 +491,10 @@ def gpu_arm(args):
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+# see the traffic note in gpu_arm
+TRAFFIC_BYTES_PER_TRAJ = (33.2e6 + 176.7e6) / 524288
 
 
 def main():

@@ -379,14 +379,14 @@ struct Lane {
   Time t, tprev, tf, t0, next_save;
   float dt, dtnew, qold, abstol, reltol;
   int cur_t, step_idx, nattempt, naccept, nreject, status;
-  bool need_begin, fsal;
 };
 
 // ------------------------------------------------------------------ Tsit5 (gpu_tsit5_perform_step.jl)
 #if DEGPU_ALG == 0
-DEGPU_DEV void begin_step(Lane& L) {
-  // FSAL: k1 = k7 of the previous step unless u was modified (:29-34, :92-97)
-  if (!L.fsal) { rhs(L.k[0], L.uprev, L.p, TP::f32(L.t)); L.fsal = true; }
+DEGPU_DEV void begin_step(Lane& L, bool first) {
+  // FSAL: k1 = k7 of the previous step unless u was modified (:29-34, :92-97); u_modified
+  // starts true, so the first step evaluates f(u0)
+  if (first) rhs(L.k[0], L.uprev, L.p, TP::f32(L.t));
   else {
 #pragma unroll
     for (int i = 0; i < N; i++) L.k[0][i] = L.k[6][i];
@@ -443,7 +443,7 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 
 // ------------------------------------------------------------------ Vern7 (gpu_vern7_perform_step.jl)
 #if DEGPU_ALG == 1
-DEGPU_DEV void begin_step(Lane& L) {
+DEGPU_DEV void begin_step(Lane& L, bool) {
   // not FSAL: k1 = f(uprev, p, t) every step (:30, :117; one evaluation per step suffices)
   rhs(L.k[0], L.uprev, L.p, TP::f32(L.t));
 }
@@ -545,7 +545,7 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 
 // ------------------------------------------------------------------ Rosenbrock23 (gpu_rosenbrock23_perform_step.jl)
 #if DEGPU_ALG == 2
-DEGPU_DEV void begin_step(Lane& L) {
+DEGPU_DEV void begin_step(Lane& L, bool) {
   // J, dT and F0 = f(uprev, t) depend only on (uprev, t): once per step (:38-49, :114-124)
   float tf_ = TP::f32(L.t);
   jacobian(L.J, L.uprev, L.p, tf_);
@@ -601,7 +601,7 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 
 // ------------------------------------------------------------------ Rodas5P (gpu_rodas5P_perform_step.jl)
 #if DEGPU_ALG == 3
-DEGPU_DEV void begin_step(Lane& L) {
+DEGPU_DEV void begin_step(Lane& L, bool) {
   float tf_ = TP::f32(L.t);  // J, dT once per step, outside the reject loop (:182-186)
   jacobian(L.J, L.uprev, L.p, tf_);
   tgrad(L.dT, L.uprev, L.p, tf_);
@@ -699,30 +699,32 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 
 #if DEGPU_ALG <= 3
 // ------------------------------------------------------------------ driver pieces (kernels.jl)
-// Output and saveat access of one lane.  With staging on (saveat runs whose L*N columns
-// fit in shared memory), saved rows go to the lane's column in shared memory and the warp
-// writes whole finished columns to HBM with coalesced stores (flush_columns); otherwise
-// rows are stored straight to global memory.  A shared saveat grid is converted to the
-// internal time type once per block (sa_s) instead of once per save.
+// Loop-invariant kernel parameters copied into registers once per thread (reading them
+// through a reference to the parameter block inside the step loop costs a constant-bank
+// load per use), plus this lane's output / saveat access.  With staging on (saveat runs
+// whose L*N columns fit in shared memory), saved rows go to the lane's column in shared
+// memory and the warp writes whole finished columns to HBM with coalesced stores
+// (flush_columns); otherwise rows are stored straight to global memory.  A shared saveat
+// grid is converted to the internal time type once per block (sa_s).
 struct Io {
   const degpu_kparams& P;
-  float* col;          // this lane's staged column (L*N floats) or nullptr
-  const Time* sa_s;    // shared saveat grid in shared memory, or nullptr
-  DEGPU_DEV Tt* ts(long long i) const { return (Tt*)P.ts + i * P.L; }
-  DEGPU_DEV float* us(long long i) const { return P.us + i * (long long)P.L * N; }
-  DEGPU_DEV Tt saveat(long long i, int l) const {
-    const Tt* s = (const Tt*)P.saveat;
-    return P.saveat_per_traj ? s[i * P.nsaveat + l] : __ldg(s + l);
+  float* col;
+  const Time* sa_s;
+  DEGPU_DEV Tt* ts(int i) const { return (Tt*)P.ts + (long long)i * P.L; }
+  DEGPU_DEV float* us(int i) const { return P.us + (long long)i * P.L * N; }
+  DEGPU_DEV Tt saveat(int i, int l) const {
+    return P.saveat_per_traj ? ((const Tt*)P.saveat)[(long long)i * P.nsaveat + l] : __ldg((const Tt*)P.saveat + l);
   }
-  DEGPU_DEV Time save_time(long long i, int l) const { return sa_s ? sa_s[l] : TP::from(saveat(i, l)); }
-  DEGPU_DEV void store_u(long long i, int l, const float* v) const {
+  DEGPU_DEV Time save_time(int i, int l) const { return sa_s ? sa_s[l] : TP::from(saveat(i, l)); }
+  DEGPU_DEV void store_u(int i, int l, const float* v) const {
     float* dst = col ? col + l * N : us(i) + (long long)l * N;
 #pragma unroll
     for (int c = 0; c < N; c++) dst[c] = v[c];
   }
 };
+DEGPU_DEV Io make_io(const degpu_kparams& P, float* col, const Time* sa_s) { return Io{P, col, sa_s}; }
 
-// Shared-memory layout of the adaptive drivers: [saveat grid (Time) | staged columns].
+// Shared-memory layout of the ODE drivers: [saveat grid (Time) | staged columns].
 struct SmemPlan {
   const Time* sa_s;
   float* cols;
@@ -744,50 +746,49 @@ DEGPU_DEV SmemPlan setup_smem(const degpu_kparams& P, char* smem) {
 
 // Warp-cooperative write of the finished lanes' staged columns (mask) and their ts
 // columns: 32 lanes store consecutive words of one trajectory's contiguous column.
-DEGPU_DEV void flush_columns(const Io& io, const float* warp_cols, unsigned mask, long long my, int my_cur, Tt my_t0) {
-  const degpu_kparams& P = io.P;
+DEGPU_DEV void flush_columns(const Io& io, const float* warp_cols, unsigned mask, int my, int my_cur, Tt my_t0) {
   const int lane = threadIdx.x & 31;
-  const int LN = P.L * N;
+  const int LN = io.P.L * N;
   __syncwarp();
   while (mask) {
     const int b = __ffs(mask) - 1;
     mask &= mask - 1;
-    const long long tr = __shfl_sync(0xffffffffu, my, b);
+    const int tr = __shfl_sync(0xffffffffu, my, b);
     const int cur = __shfl_sync(0xffffffffu, my_cur, b);
     const Tt t0 = __shfl_sync(0xffffffffu, my_t0, b);
     const float* src = warp_cols + b * LN;
-    float* dst = P.us + tr * (long long)LN;
+    float* dst = io.P.us + (long long)tr * LN;
     for (int k = lane; k < LN; k += 32)
       if (k < cur * N) dst[k] = src[k];  // rows never saved stay untouched, like the reference's
-    Tt* ts = (Tt*)P.ts + tr * P.L;
-    for (int l = lane; l < P.L; l += 32) ts[l] = (l < cur) ? io.saveat(tr, l) : t0;
+    Tt* ts = io.ts(tr);
+    for (int l = lane; l < io.P.L; l += 32) ts[l] = (l < cur) ? io.saveat(tr, l) : t0;
   }
   __syncwarp();
 }
 
-// init (nonstiff/types.jl:340-402 et al.) + initial save (kernels.jl:116-126)
-DEGPU_DEV void lane_init(Lane& L, const Io& io, long long i) {
-  const degpu_kparams& P = io.P;
-  const Tt* tsp = (const Tt*)P.tspan + 2 * i;
+// init (nonstiff/types.jl:340-402 et al.) + initial save (kernels.jl:116-126), and the
+// first step's set-up (k1 = f(u0) for the FSAL methods: u_modified starts true)
+DEGPU_DEV void lane_init(Lane& L, const Io& io, int i) {
+  const Tt* tsp = ((const Tt*)io.P.tspan) + 2 * (long long)i;
   const Tt t0_in = tsp[0];
   L.t0 = TP::from(t0_in);
   L.tf = TP::from(tsp[1]);
   L.t = L.t0;
   L.tprev = L.t0;
 #pragma unroll
-  for (int c = 0; c < N; c++) { L.u[c] = P.u0[i * N + c]; L.uprev[c] = L.u[c]; }
+  for (int c = 0; c < N; c++) { L.u[c] = io.P.u0[(long long)i * N + c]; L.uprev[c] = L.u[c]; }
 #pragma unroll
-  for (int c = 0; c < NP; c++) L.p[c] = (c < DEGPU_P) ? P.p[i * DEGPU_P + c] : 0.0f;
+  for (int c = 0; c < NP; c++) L.p[c] = (c < DEGPU_P) ? io.P.p[(long long)i * DEGPU_P + c] : 0.0f;
 #pragma unroll
   for (int s = 0; s < NK; s++)
 #pragma unroll
     for (int c = 0; c < N; c++) L.k[s][c] = L.u[c];
-  float dt = P.dt0 ? P.dt0[i] : (float)(Tt)P.dt;
+  float dt = io.P.dt0 ? io.P.dt0[i] : (float)(Tt)io.P.dt;
   L.dt = dt;
   L.dtnew = dt;
-  float sc = P.tolscale ? P.tolscale[i] : 1.0f;
-  L.abstol = P.abstol * sc;
-  L.reltol = P.reltol * sc;
+  float sc = io.P.tolscale ? io.P.tolscale[i] : 1.0f;
+  L.abstol = io.P.abstol * sc;
+  L.reltol = io.P.reltol * sc;
   L.qold = (float)1.0e-4;
   L.cur_t = 0;
   L.step_idx = 1;
@@ -795,34 +796,32 @@ DEGPU_DEV void lane_init(Lane& L, const Io& io, long long i) {
   L.naccept = 0;
   L.nreject = 0;
   L.status = DEGPU_RET_DEFAULT;
-  L.need_begin = true;
-  L.fsal = false;
-  if (P.nsaveat) {
+  if (io.P.nsaveat) {
     const Tt s0 = io.saveat(i, 0);
     if (t0_in == s0) { L.cur_t = 1; io.store_u(i, 0, L.u); }
-    L.next_save = io.save_time(i, L.cur_t < P.nsaveat ? L.cur_t : 0);
+    L.next_save = io.save_time(i, L.cur_t < io.P.nsaveat ? L.cur_t : 0);
   } else {
     io.store_u(i, 0, L.u);
   }
+  begin_step(L, true);
 }
 
 // savevalues! (integrator_utils.jl:13-50)
-DEGPU_DEV void save_values(Lane& L, const Io& io, long long i, bool save_everystep) {
-  const degpu_kparams& P = io.P;
-  if (P.nsaveat) {
+DEGPU_DEV void save_values(Lane& L, const Io& io, int i, bool save_everystep) {
+  if (io.P.nsaveat) {
     // the next save time is cached in registers: one compare per step, no global load
-    while (L.cur_t < P.nsaveat && TP::le(L.next_save, L.t)) {
+    while (L.cur_t < io.P.nsaveat && TP::le(L.next_save, L.t)) {
       float th = TP::theta(L.next_save, L.tprev, L.dt);
-      if (L.cur_t < P.L) {
+      if (L.cur_t < io.P.L) {
         float v[N];
         interp(L, th, L.dt, v);
         io.store_u(i, L.cur_t, v);
       }
       L.cur_t++;
-      if (L.cur_t < P.nsaveat) L.next_save = io.save_time(i, L.cur_t);
+      if (L.cur_t < io.P.nsaveat) L.next_save = io.save_time(i, L.cur_t);
     }
   } else if (save_everystep) {
-    if (L.step_idx < P.L) { io.store_u(i, L.step_idx, L.u); io.ts(i)[L.step_idx] = TP::out(L.t); }
+    if (L.step_idx < io.P.L) { io.store_u(i, L.step_idx, L.u); io.ts(i)[L.step_idx] = TP::out(L.t); }
     L.step_idx++;
   }
 }
@@ -850,22 +849,18 @@ DEGPU_DEV bool controller(Lane& L, float EEst, float& dt, Time t) {
   return true;
 }
 
-// One attempt of step!.  Returns true when the trajectory is finished.
+// One attempt of step!.  Returns true when the trajectory is finished.  After an accepted
+// step that does not finish the span, the next step is set up right away (uprev = u,
+// FSAL k1 / k1 = f(u) / Jacobian), so the attempt path itself carries no set-up branch;
+// after the final step uprev and the stages are kept for the end-of-span interpolation.
 template <bool ADAPTIVE>
-DEGPU_DEV bool advance(Lane& L, const Io& io, long long i) {
-  const degpu_kparams& P = io.P;
-  if (L.need_begin) {
-#pragma unroll
-    for (int c = 0; c < N; c++) L.uprev[c] = L.u[c];
-    begin_step(L);
-    L.need_begin = false;
-  }
-  Time t = L.t;
+DEGPU_DEV bool advance(Lane& L, const Io& io, int i) {
+  const Time t = L.t;
   float unew[N], err[N];
   if (ADAPTIVE) {
     float dt = L.dtnew;
     if (dt < 1.0e-14f) { L.status = DEGPU_RET_DTLESSTHANMIN; return true; }
-    if (++L.nattempt > P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
+    if (++L.nattempt > io.P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
     attempt<true>(L, t, dt, unew, err);
     float EEst = scaled_norm(err, L.uprev, unew, L.abstol, L.reltol);
 #if !DEGPU_PARITY
@@ -878,9 +873,9 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, long long i) {
       L.nreject++;
       return false;
     }
-    if (L.naccept == 0 && P.dt_first) P.dt_first[i] = dt;
+    if (L.naccept == 0 && io.P.dt_first) io.P.dt_first[i] = dt;
   } else {
-    if (++L.nattempt > P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
+    if (++L.nattempt > io.P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
     float dt = L.dt;
     L.tprev = t;
     L.t = TP::add(t, dt);
@@ -889,30 +884,34 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, long long i) {
 #pragma unroll
   for (int c = 0; c < N; c++) L.u[c] = unew[c];
   L.naccept++;
-  L.need_begin = true;
-  save_values(L, io, i, !ADAPTIVE && P.save_everystep);
-  return !TP::lt(L.t, L.tf);
+  save_values(L, io, i, !ADAPTIVE && io.P.save_everystep);
+  const bool done = !TP::lt(L.t, L.tf);
+  if (!done) {
+#pragma unroll
+    for (int c = 0; c < N; c++) L.uprev[c] = L.u[c];
+    begin_step(L, false);
+  }
+  return done;
 }
 
 // end of the driver loop (kernels.jl:53-62, 133-142) and outputs
-DEGPU_DEV void lane_finish(Lane& L, const Io& io, long long i) {
-  const degpu_kparams& P = io.P;
+DEGPU_DEV void lane_finish(Lane& L, const Io& io, int i) {
   Tt* ts = io.ts(i);
-  const Tt t0_in = ((const Tt*)P.tspan)[2 * i];  // fill! ts with tspan[1] (lowerlevel_solve.jl:82)
-  if (P.nsaveat) {
+  const Tt t0_in = ((const Tt*)io.P.tspan)[2 * (long long)i];  // fill! ts with tspan[1] (lowerlevel_solve.jl:82)
+  if (io.P.nsaveat) {
     if (!io.col)  // staged columns are written by flush_columns
-      for (int l = 0; l < P.L; l++) ts[l] = (l < L.cur_t) ? io.saveat(i, l) : t0_in;
+      for (int l = 0; l < io.P.L; l++) ts[l] = (l < L.cur_t) ? io.saveat(i, l) : t0_in;
   } else {
-    int first_unset = P.save_everystep ? (L.step_idx < P.L ? L.step_idx : P.L) : 1;
+    int first_unset = io.P.save_everystep ? (L.step_idx < io.P.L ? L.step_idx : io.P.L) : 1;
     ts[0] = t0_in;
-    for (int l = first_unset; l < P.L; l++) ts[l] = t0_in;
-    if (TP::lt(L.tf, L.t) && P.save_everystep) {
+    for (int l = first_unset; l < io.P.L; l++) ts[l] = t0_in;
+    if (TP::lt(L.tf, L.t) && io.P.save_everystep) {
       float v[N];
       interp(L, TP::theta(L.tf, L.tprev, L.dt), L.dt, v);
-      io.store_u(i, P.L - 1, v);
-      ts[P.L - 1] = ((const Tt*)P.tspan)[2 * i + 1];
+      io.store_u(i, io.P.L - 1, v);
+      ts[io.P.L - 1] = ((const Tt*)io.P.tspan)[2 * (long long)i + 1];
     }
-    if (!P.save_everystep) { io.store_u(i, 1, L.u); ts[1] = TP::out(L.t); }
+    if (!io.P.save_everystep) { io.store_u(i, 1, L.u); ts[1] = TP::out(L.t); }
   }
   if (L.status == DEGPU_RET_DEFAULT) {
     bool fin = true;
@@ -920,9 +919,9 @@ DEGPU_DEV void lane_finish(Lane& L, const Io& io, long long i) {
     for (int c = 0; c < N; c++) fin = fin && isfinite(L.u[c]);
     L.status = fin ? DEGPU_RET_SUCCESS : DEGPU_RET_UNSTABLE;
   }
-  if (P.retcode) P.retcode[i] = (signed char)L.status;
-  if (P.naccept) P.naccept[i] = L.naccept;
-  if (P.nreject) P.nreject[i] = L.nreject;
+  if (io.P.retcode) io.P.retcode[i] = (signed char)L.status;
+  if (io.P.naccept) io.P.naccept[i] = L.naccept;
+  if (io.P.nreject) io.P.nreject[i] = L.nreject;
 }
 #endif  // DEGPU_ALG <= 3
 
@@ -935,10 +934,11 @@ extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCK
   using namespace degpu;
   extern __shared__ __align__(16) char smem[];
   const SmemPlan sp = setup_smem(P, smem);
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < P.B;
+  const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = gi < P.B;
+  const int i = (int)gi;
   float* warp_cols = sp.cols ? sp.cols + (threadIdx.x & ~31) * P.L * N : nullptr;
-  Io io{P, sp.cols ? warp_cols + (threadIdx.x & 31) * P.L * N : nullptr, sp.sa_s};
+  const Io io = make_io(P, sp.cols ? warp_cols + (threadIdx.x & 31) * P.L * N : nullptr, sp.sa_s);
   Lane L;
   if (valid) {
     lane_init(L, io, i);
@@ -948,7 +948,7 @@ extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCK
   }
   if (sp.cols) {
     const unsigned m = __ballot_sync(0xffffffffu, valid);
-    flush_columns(io, warp_cols, m, i, valid ? L.cur_t : 0, valid ? ((const Tt*)P.tspan)[2 * i] : (Tt)0);
+    flush_columns(io, warp_cols, m, i, valid ? L.cur_t : 0, valid ? ((const Tt*)io.P.tspan)[2 * gi] : (Tt)0);
   }
 }
 #endif
@@ -960,7 +960,7 @@ extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCK
 // stepping while trajectories of very different lengths (uneven step counts, per-
 // trajectory tspans) drain.  Every trajectory is bounded by maxiters attempts, so the
 // loop ends: each pass either advances some lane or hands out work, and no lane ever
-// waits on another warp or block.
+// waits on another warp or block.  (The host limits B to 2^31 - 1, so indices are int.)
 extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCKS) degpu_persistent_kernel(const degpu_kparams P) {
   using namespace degpu;
   const unsigned FULL = 0xffffffffu;
@@ -969,38 +969,39 @@ extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCK
   extern __shared__ __align__(16) char smem[];
   const SmemPlan sp = setup_smem(P, smem);
   float* warp_cols = sp.cols ? sp.cols + (threadIdx.x & ~31) * P.L * N : nullptr;
-  Io io{P, sp.cols ? warp_cols + lane * P.L * N : nullptr, sp.sa_s};
-  Lane L;
-  long long my = -1;
-  long long q_next = 0, q_end = 0;
-  bool exhausted = false;
-  const long long B = P.B;
+  const Io io = make_io(P, sp.cols ? warp_cols + lane * P.L * N : nullptr, sp.sa_s);
+  unsigned long long* const work = P.work;
+  const int B = (int)P.B;
   const int chunk = P.chunk > 0 ? P.chunk : 32;
+  Lane L;
+  int my = -1;
+  int q_next = 0, q_end = 0;
+  bool exhausted = false;
   for (;;) {
     bool fin = false;
-    unsigned idle = __ballot_sync(FULL, my < 0);
+    const unsigned idle = __ballot_sync(FULL, my < 0);
     if (idle) {
       if (q_next >= q_end && !exhausted) {
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(P.work, (unsigned long long)chunk);
+        if (lane == 0) base = atomicAdd(work, (unsigned long long)chunk);
         base = __shfl_sync(FULL, base, 0);
-        if ((long long)base >= B) exhausted = true;
-        else { q_next = (long long)base; q_end = min((long long)base + chunk, B); }
+        if (base >= (unsigned long long)B) exhausted = true;
+        else { q_next = (int)base; q_end = min((int)base + chunk, B); }
       }
-      int rank = __popc(idle & lt_mask);
+      const int rank = __popc(idle & lt_mask);
       if (my < 0 && q_next + rank < q_end) {
         my = q_next + rank;
         lane_init(L, io, my);
         if (!TP::lt(L.t, L.tf)) { lane_finish(L, io, my); fin = true; }
       }
-      q_next = min(q_next + (long long)__popc(idle), q_end);
+      q_next = min(q_next + __popc(idle), q_end);
     }
     if (my >= 0 && !fin) {
       if (advance<true>(L, io, my)) { lane_finish(L, io, my); fin = true; }
     }
     if (sp.cols) {
       const unsigned fm = __ballot_sync(FULL, fin);
-      if (fm) flush_columns(io, warp_cols, fm, my, fin ? L.cur_t : 0, fin ? ((const Tt*)P.tspan)[2 * my] : (Tt)0);
+      if (fm) flush_columns(io, warp_cols, fm, my, fin ? L.cur_t : 0, fin ? ((const Tt*)io.P.tspan)[2 * (long long)my] : (Tt)0);
     }
     if (fin) my = -1;
     if (__ballot_sync(FULL, my >= 0) == 0 && exhausted) break;
