@@ -97,28 +97,36 @@ def compile_lib(verbose: bool = False) -> Path:
     return LIB
 
 
-CHECKS = [  # (alg, driver, time type, parity) instantiations compiled by the build check
-    (0, 0, "float", 1), (0, 1, "double", 0), (0, 2, "double", 0), (1, 2, "double", 0),
-    (2, 2, "double", 0), (3, 2, "double", 0), (3, 1, "double", 1),
+CHECKS = [  # (alg, driver, time type, parity, model, extra defines) compiled by the build check
+    (0, 0, "float", 1, "lorenz", ""), (0, 1, "double", 0, "lorenz", ""), (0, 2, "double", 0, "lorenz", ""),
+    (1, 2, "double", 0, "lorenz", ""), (2, 2, "double", 0, "lorenz", ""), (3, 2, "double", 0, "lorenz", ""),
+    (3, 1, "double", 1, "lorenz", ""),
+    # tstops + callbacks: continuous (bouncing ball) and discrete (decay) sets
+    (0, 2, "double", 0, "ball", "-DDEGPU_NCCB=2 -DDEGPU_TSTOPS=1"),
+    (1, 0, "float", 1, "decay", "-DDEGPU_NDCB=2 -DDEGPU_TSTOPS=1"),
 ]
+MODEL_DIMS = {"lorenz": (3, 3), "ball": (2, 1), "decay": (1, 1)}
 
 
 def check_kernels(verbose: bool = False) -> list[str]:
-    """Compile representative kernel instantiations with nvcc (Lorenz RHS); returns ptxas lines."""
+    """Compile representative kernel instantiations with nvcc; returns ptxas lines."""
     BUILD.mkdir(exist_ok=True)
-    tu = BUILD / "kernel_check.cu"
-    tu.write_text('#include "degpu_prelude.cuh"\n#include "lorenz.cuh"\n#include "degpu_kernels.cuh"\n')
 
     def one(c):
-        alg, drv, tt, par = c
+        alg, drv, tt, par, model, extra = c
+        n, p = MODEL_DIMS[model]
+        tag = f"{alg}_{drv}_{tt}_{par}_{model}_{len(extra)}"
+        tu = BUILD / f"kernel_check_{tag}.cu"
+        tu.write_text(f'#include "degpu_prelude.cuh"\n#include "{model}.cuh"\n#include "degpu_kernels.cuh"\n')
         cmd = [NVCC, "-std=c++17", *ARCH, "-Xptxas", "-v", "-c", str(tu), "-o", os.devnull,
                "-I", str(CSRC / "device"), "-I", str(CSRC / "models"),
-               f"-DDEGPU_N=3", f"-DDEGPU_P=3", f"-DDEGPU_ALG={alg}", f"-DDEGPU_DRIVER={drv}", f"-DDEGPU_TT={tt}",
+               f"-DDEGPU_N={n}", f"-DDEGPU_P={p}", f"-DDEGPU_ALG={alg}", f"-DDEGPU_DRIVER={drv}", f"-DDEGPU_TT={tt}",
                f"-DDEGPU_PARITY={par}", "-DDEGPU_JAC=0", "-DDEGPU_TGRAD=0", "-DDEGPU_LINSOLVE_REFINE=1",
-               f"-DDEGPU_TIME_DF={1 if tt == 'double' else 0}"]
+               f"-DDEGPU_TIME_DF={1 if tt == 'double' else 0}", *extra.split()]
         cmd += ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"] if par else ["-prec-div=false", "-prec-sqrt=false"]
         log = _run(cmd)
-        return [f"alg={alg} driver={drv} tt={tt} parity={par}: {ln.strip()}" for ln in log.splitlines() if "registers" in ln]
+        return [f"alg={alg} driver={drv} tt={tt} parity={par} {model} {extra}: {ln.strip()}"
+                for ln in log.splitlines() if "registers" in ln]
 
     out = []
     with ThreadPoolExecutor(max_workers=len(CHECKS)) as ex:

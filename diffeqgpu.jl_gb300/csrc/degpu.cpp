@@ -119,9 +119,11 @@ namespace {
 
 struct KernelSpec {
   int alg, driver, tt, parity, jac, tgrad, refine;
+  int tstops = 0, nccb = 0, ndcb = 0;  // tstops / callback set compiled into the kernel
   std::string key() const {
-    char b[128];
-    snprintf(b, sizeof b, "a%d_d%d_t%d_m%d_j%d_g%d_r%d", alg, driver, tt, parity, jac, tgrad, refine);
+    char b[160];
+    snprintf(b, sizeof b, "a%d_d%d_t%d_m%d_j%d_g%d_r%d_s%d_c%d_e%d", alg, driver, tt, parity, jac, tgrad, refine,
+             tstops, nccb, ndcb);
     return b;
   }
 };
@@ -158,12 +160,14 @@ void mkdirs(const std::string& path) {
 }
 
 std::string build_source(const degpu_rhs_s* f, const KernelSpec& k) {
-  char defs[512];
+  char defs[640];
   snprintf(defs, sizeof defs,
            "#define DEGPU_N %d\n#define DEGPU_P %d\n#define DEGPU_TT %s\n#define DEGPU_ALG %d\n"
            "#define DEGPU_DRIVER %d\n#define DEGPU_PARITY %d\n#define DEGPU_JAC %d\n#define DEGPU_TGRAD %d\n"
-           "#define DEGPU_LINSOLVE_REFINE %d\n#define DEGPU_TIME_DF %d\n",
-           f->N, f->P, k.tt ? "double" : "float", k.alg, k.driver, k.parity, k.jac, k.tgrad, k.refine, k.tt);
+           "#define DEGPU_LINSOLVE_REFINE %d\n#define DEGPU_TIME_DF %d\n"
+           "#define DEGPU_TSTOPS %d\n#define DEGPU_NCCB %d\n#define DEGPU_NDCB %d\n",
+           f->N, f->P, k.tt ? "double" : "float", k.alg, k.driver, k.parity, k.jac, k.tgrad, k.refine, k.tt,
+           k.tstops, k.nccb, k.ndcb);
   std::string s = defs;
   // developer override of the drivers' launch bounds (register budget experiments)
   if (const char* lb = getenv("DEGPU_LB")) {
@@ -377,6 +381,35 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   P.nsaveat = o->nsaveat;
   P.saveat_per_traj = o->saveat_per_traj;
   P.save_everystep = o->save_everystep;
+  // tstops and callbacks (vectorized_(a)solve kwargs tstops / callback)
+  if (o->ntstops < 0) return fail(DEGPU_E_INVALID, "ntstops < 0");
+  if (o->ntstops > 0 && !o->tstops) return fail(DEGPU_E_INVALID, "tstops pointer missing");
+  const degpu_callbacks* cb = o->callbacks;
+  const int nc = cb ? cb->n_continuous : 0, nd = cb ? cb->n_discrete : 0;
+  if (nc < 0 || nd < 0 || nc > DEGPU_MAX_CALLBACKS || nd > DEGPU_MAX_CALLBACKS)
+    return fail(DEGPU_E_INVALID, "at most 8 continuous and 8 discrete callbacks per set");
+  if ((nc && !cb->continuous) || (nd && !cb->discrete)) return fail(DEGPU_E_INVALID, "callback array missing");
+  if (o->alg == DEGPU_ALG_EM && (nc || nd || o->ntstops))
+    return fail(DEGPU_E_UNSUPPORTED, "GPUEM takes no callbacks or tstops (em_kernel, gpu_em_perform_step.jl)");
+  for (int j = 0; j < nc; j++) {
+    const degpu_continuous_callback& c = cb->continuous[j];
+    if (c.fn < 0 || c.rootfind < 0 || c.rootfind > 2 || !(c.abstol >= 0.0) || !(c.dtrelax > 0.0))
+      return fail(DEGPU_E_INVALID, "bad continuous callback (fn >= 0, rootfind in 0..2, abstol >= 0, dtrelax > 0)");
+    P.ccb_fn[j] = c.fn;
+    P.ccb_flags[j] = (c.has_affect ? 1 : 0) | (c.has_affect_neg ? 2 : 0) | (c.rootfind << 2);
+    P.ccb_abstol[j] = (float)c.abstol;
+    P.ccb_nudge[j] = (float)c.repeat_nudge;
+    P.ccb_dtrelax[j] = (float)c.dtrelax;
+  }
+  for (int j = 0; j < nd; j++) {
+    if (cb->discrete[j] < 0) return fail(DEGPU_E_INVALID, "bad discrete callback function index");
+    P.dcb_fn[j] = cb->discrete[j];
+  }
+  P.ntstops = o->ntstops;
+  P.tstops = o->ntstops ? o->tstops : nullptr;
+  k.tstops = o->ntstops > 0 ? 1 : 0;
+  k.nccb = nc;
+  k.ndcb = nd;
   rq->block = o->block;
   rq->chunk = o->chunk;
   return 0;
@@ -479,6 +512,13 @@ int run(const degpu_rhs* f, const degpu_problems* pr, const degpu_options* o, in
 extern "C" {
 
 const char* degpu_version(void) { return DEGPU_VERSION; }
+void degpu_abi_struct_sizes(int* options, int* outputs, int* problems, int* continuous_callback, int* callbacks) {
+  if (options) *options = (int)sizeof(degpu_options);
+  if (outputs) *outputs = (int)sizeof(degpu_outputs);
+  if (problems) *problems = (int)sizeof(degpu_problems);
+  if (continuous_callback) *continuous_callback = (int)sizeof(degpu_continuous_callback);
+  if (callbacks) *callbacks = (int)sizeof(degpu_callbacks);
+}
 const char* degpu_last_error(void) { return g_err.c_str(); }
 
 int degpu_rhs_create(const char* cuda_source, int n_state, int n_param, int flags, degpu_rhs** out) {

@@ -80,6 +80,21 @@ struct TP {
 typedef TP::T Time;
 constexpr int NP = DEGPU_P > 0 ? DEGPU_P : 1;
 
+// tstops and callbacks are compiled in only when a solve asks for them:
+//   DEGPU_TSTOPS  1 = the solve has tstops
+//   DEGPU_NCCB    number of continuous callbacks in the set (GPUContinuousCallback)
+//   DEGPU_NDCB    number of discrete callbacks in the set (GPUDiscreteCallback)
+#ifndef DEGPU_TSTOPS
+#define DEGPU_TSTOPS 0
+#endif
+#ifndef DEGPU_NCCB
+#define DEGPU_NCCB 0
+#endif
+#ifndef DEGPU_NDCB
+#define DEGPU_NDCB 0
+#endif
+#define DEGPU_CALLBACKS (DEGPU_NCCB > 0 || DEGPU_NDCB > 0)
+
 #if DEGPU_ALG == 0
 constexpr int NK = 7;
 constexpr int ORDER = 5;
@@ -379,6 +394,13 @@ struct Lane {
   Time t, tprev, tf, t0, next_save;
   float dt, dtnew, qold, abstol, reltol;
   int cur_t, step_idx, nattempt, naccept, nreject, status;
+#if DEGPU_TSTOPS
+  int tstops_idx;         // next tstop (0-based integ.tstops_idx)
+#endif
+#if DEGPU_NCCB > 0
+  int event_last;         // event_last_time: 1-based index of the last event's callback, 0 = none
+  float last_event_error; // condition residual at the last located event
+#endif
 };
 
 // ------------------------------------------------------------------ Tsit5 (gpu_tsit5_perform_step.jl)
@@ -803,6 +825,13 @@ DEGPU_DEV void lane_init(Lane& L, const Io& io, int i) {
   } else {
     io.store_u(i, 0, L.u);
   }
+#if DEGPU_TSTOPS
+  L.tstops_idx = 0;
+#endif
+#if DEGPU_NCCB > 0
+  L.event_last = 1;  // integrator init: event_last_time = 1, last_event_error = 0 (stiff/types.jl:44-46)
+  L.last_event_error = 0.0f;
+#endif
   begin_step(L, true);
 }
 
@@ -849,6 +878,236 @@ DEGPU_DEV bool controller(Lane& L, float EEst, float& dt, Time t) {
   return true;
 }
 
+// ------------------------------------------------------------------ tstops
+#if DEGPU_TSTOPS
+// `tstops[idx] - t - dt - 100 eps(T) < 0` (gpu_tsit5_perform_step.jl:18-19, :158-160 and the
+// same test in every other perform_step file), in the time type's arithmetic.
+constexpr float kTstopTol = sizeof(Tt) == 8 ? (float)(100.0 * 2.220446049250313e-16) : 100.0f * 1.1920928955078125e-07f;
+DEGPU_DEV bool tstop_due(const Lane& L, const Io& io, Time t, float dt, Time& s) {
+  if (L.tstops_idx >= io.P.ntstops) return false;
+  s = TP::from(((const Tt*)io.P.tstops)[L.tstops_idx]);
+  return TP::rem(s, t, dt) - kTstopTol < 0.0f;
+}
+#endif
+
+// ------------------------------------------------------------------ callbacks
+// GPUContinuousCallback / GPUDiscreteCallback handling of integrator_utils.jl:52-479.  The
+// user's source defines, for a set with continuous callbacks,
+//   float degpu_ccb_condition(int fn, const float* u, const float* p, degpu_time t)
+//   void  degpu_ccb_affect(int fn, degpu_integrator& I), degpu_ccb_affect_neg(int fn, ...)
+// and, with discrete callbacks,
+//   bool  degpu_dcb_condition(int fn, const float* u, const float* p, degpu_time t)
+//   void  degpu_dcb_affect(int fn, degpu_integrator& I)
+// where fn is the function index the callback set assigns to each member.
+#if DEGPU_CALLBACKS
+DEGPU_DEV void run_affect(Lane& L, int kind, int fn) {
+  degpu_integrator I;
+  I.u = L.u;
+  I.p = L.p;
+  I.t = (Tt)TP::out(L.t);
+  I.dt = L.dt;
+  I.terminated = 0;
+#if DEGPU_NCCB > 0
+  if (kind == 0) degpu_ccb_affect(fn, I);
+  else if (kind == 1) degpu_ccb_affect_neg(fn, I);
+#endif
+#if DEGPU_NDCB > 0
+  if (kind == 2) degpu_dcb_affect(fn, I);
+#endif
+  if (I.terminated) L.status = DEGPU_RET_TERMINATED;  // terminate! (integrator_utils.jl:52-65)
+}
+#endif
+
+#if DEGPU_NCCB > 0
+// Julia's sign / eps / nextfloat / max on the time type (ITP root finder)
+DEGPU_DEV float jl_sign(float x) { return (x == 0.0f || x != x) ? x : copysignf(1.0f, x); }
+DEGPU_DEV float t_abs(float x) { return fabsf(x); }
+DEGPU_DEV double t_abs(double x) { return fabs(x); }
+DEGPU_DEV float t_copysign(float a, float b) { return copysignf(a, b); }
+DEGPU_DEV double t_copysign(double a, double b) { return copysign(a, b); }
+DEGPU_DEV float t_max(float x, float y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
+DEGPU_DEV double t_max(double x, double y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
+DEGPU_DEV float t_eps(float x) {  // ldexp(eps(T), exponent(x)); nextfloat(0) below floatmin
+  const unsigned e = (__float_as_uint(x) >> 23) & 0xffu;
+  if (e == 0xffu) return __uint_as_float(0x7fc00000u);
+  if (e > 23u) return __uint_as_float((e - 23u) << 23);
+  return __uint_as_float(e == 0u ? 1u : (1u << (e - 1u)));
+}
+DEGPU_DEV double t_eps(double x) {
+  const unsigned long long e = ((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffull;
+  if (e == 0x7ffull) return __longlong_as_double(0x7ff8000000000000ll);
+  if (e > 52ull) return __longlong_as_double((long long)((e - 52ull) << 52));
+  return __longlong_as_double((long long)(e == 0ull ? 1ull : (1ull << (e - 1ull))));
+}
+DEGPU_DEV float t_nextfloat(float x) {
+  if (x != x || x == __int_as_float(0x7f800000)) return x;
+  if (x == 0.0f) return __uint_as_float(1u);
+  const unsigned b = __float_as_uint(x);
+  return __uint_as_float(x > 0.0f ? b + 1u : b - 1u);
+}
+DEGPU_DEV double t_nextfloat(double x) {
+  if (x != x || x == __longlong_as_double(0x7ff0000000000000ll)) return x;
+  if (x == 0.0) return __longlong_as_double(1ll);
+  const long long b = __double_as_longlong(x);
+  return __longlong_as_double(x > 0.0 ? b + 1 : b - 1);
+}
+
+// get_condition (integrator_utils.jl:461-479): u at t, uprev at tprev, else integ(abst)
+DEGPU_DEV float ccb_condition_at(const Lane& L, int fn, Tt abst) {
+  float x[N];
+  if (abst == (Tt)TP::out(L.t)) {
+#pragma unroll
+    for (int c = 0; c < N; c++) x[c] = L.u[c];
+  } else if (abst == (Tt)TP::out(L.tprev)) {
+#pragma unroll
+    for (int c = 0; c < N; c++) x[c] = L.uprev[c];
+  } else {
+    interp(L, TP::theta(TP::from(abst), L.tprev, L.dt), L.dt, x);
+  }
+  return (float)degpu_ccb_condition(fn, x, L.p, abst);
+}
+
+// gpu_find_root (integrator_utils.jl:302-355): ITP with scaled_k1 = 0.2, k2 = 2, n0 = 10,
+// at most 100 iterations, in the time type
+DEGPU_DEV Tt itp_root(const Lane& L, int fn, Tt left, Tt right, int rootfind) {
+  float fl = ccb_condition_at(L, fn, left);
+  float fr = ccb_condition_at(L, fn, right);
+  const Tt span0 = right - left;
+  const Tt k1 = (Tt)0.2 / span0;
+  Tt eps_s = span0 * (Tt)512;
+  for (int it = 0; it < 100; it++) {
+    const Tt span = right - left;
+    const Tt mid = (left + right) / (Tt)2;
+    const Tt r = eps_s - span / (Tt)2;
+    const Tt x_f = left + (span * (Tt)fl) / (Tt)(fl - fr);
+    const Tt delta = t_max(k1 * span * span, t_eps(x_f));
+    const Tt diff = mid - x_f;
+    const Tt xt = (delta <= t_abs(diff)) ? x_f + t_copysign(delta, diff) : mid;
+    const Tt xp = (t_abs(xt - mid) <= r) ? xt : mid - t_copysign(r, diff);
+    const float yp = ccb_condition_at(L, fn, xp);
+    const float yps = yp * jl_sign(fr);
+    if (yps > 0.0f) { right = xp; fr = yp; }
+    else if (yps < 0.0f) { left = xp; fl = yp; }
+    else { left = xp; right = xp; break; }
+    eps_s = eps_s / (Tt)2;
+    if (t_nextfloat(left) >= right) break;
+  }
+  return rootfind == 1 ? right : left;  // SciMLBase.RightRootFind : LeftRootFind
+}
+
+struct CbEvent {
+  Tt t;
+  float prev_sign, residual;
+  bool occurred;
+};
+// find_callback_time (integrator_utils.jl:357-428) for member j of the set
+DEGPU_DEV CbEvent find_callback_time(const Lane& L, const Io& io, int j) {
+  const int fn = io.P.ccb_fn[j], fl = io.P.ccb_flags[j];
+  float x[N];
+#pragma unroll
+  for (int c = 0; c < N; c++) x[c] = L.uprev[c];
+  Tt bottom_t = (Tt)TP::out(L.tprev);
+  float bottom_c = (float)degpu_ccb_condition(fn, x, L.p, bottom_t);
+  if (L.event_last == j + 1 && fabsf(bottom_c - L.last_event_error) <= io.P.ccb_abstol[j]) {
+    // nudge past the previous event's root so that it is not found again
+    bottom_t = bottom_t + (Tt)(L.dt * io.P.ccb_nudge[j]);
+    bottom_c = ccb_condition_at(L, fn, bottom_t);
+  }
+  const float bs = jl_sign(bottom_c);
+  const Tt top_t = (Tt)TP::out(L.t);
+  const float ts_ = jl_sign(ccb_condition_at(L, fn, top_t));
+  CbEvent e;
+  e.prev_sign = bs;
+  e.t = top_t;
+  e.residual = 0.0f;
+  e.occurred = ((bs < 0.0f && (fl & 1)) || (bs > 0.0f && (fl & 2))) && bs * ts_ <= 0.0f;
+  const int rootfind = (fl >> 2) & 3;
+  if (e.occurred && rootfind != 2 && ts_ != 0.0f) {
+    e.t = itp_root(L, fn, bottom_t, top_t, rootfind);
+    e.residual = ccb_condition_at(L, fn, e.t);
+  }
+  return e;
+}
+
+// change_t_via_interpolation! (integrator_utils.jl:180-209)
+DEGPU_DEV void change_t_via_interpolation(Lane& L, Tt tnew) {
+  const Tt tcur = (Tt)TP::out(L.t);
+  if (tnew != tcur) {
+    float v[N];
+    interp(L, TP::theta(TP::from(tnew), L.tprev, L.dt), L.dt, v);
+#pragma unroll
+    for (int c = 0; c < N; c++) L.u[c] = v[c];
+    L.step_idx -= (int)rint((tcur - tnew) / (Tt)L.dt);
+    L.t = TP::from(tnew);
+  }
+}
+#endif
+
+#if DEGPU_CALLBACKS
+// handle_callbacks! (integrator_utils.jl:258-300): the earliest continuous event is applied
+// with apply_callback! (:212-256) -- which, like the reference, runs the affect of the
+// set's FIRST continuous callback -- then every discrete callback in order
+// (apply_discrete_callback!, :67-150).  Returns saved_in_cb; u_mod is u_modified.
+template <bool ADAPTIVE>
+DEGPU_DEV bool handle_callbacks(Lane& L, const Io& io, int i, bool save_every, bool& u_mod) {
+  bool saved = false;
+#if DEGPU_NCCB > 0
+  CbEvent best;
+  best.occurred = false;
+  best.t = (Tt)0;
+  best.prev_sign = 0.0f;
+  best.residual = 0.0f;
+  int idx = 0;
+#pragma unroll
+  for (int j = 0; j < DEGPU_NCCB; j++) {
+    const CbEvent e = find_callback_time(L, io, j);
+    if (e.occurred && (!best.occurred || e.t < best.t)) { best = e; idx = j + 1; }
+  }
+  if (best.occurred) {
+    L.event_last = idx;
+    L.last_event_error = best.residual;
+    change_t_via_interpolation(L, best.t);
+    if (ADAPTIVE && L.dtnew < 1.0e-12f) {
+      const Tt remaining = t_abs((Tt)TP::out(L.tf) - (Tt)TP::out(L.t));
+      const Tt relaxed = (Tt)(io.P.ccb_dtrelax[0] * L.dt);
+      L.dtnew = (float)((remaining < relaxed) ? remaining : relaxed);
+    }
+    save_values(L, io, i, save_every);
+    saved = true;
+    u_mod = true;
+    const int f0 = io.P.ccb_flags[0];
+    if (best.prev_sign < 0.0f) {
+      if (f0 & 1) run_affect(L, 0, io.P.ccb_fn[0]);
+      else u_mod = false;
+    } else if (best.prev_sign > 0.0f) {
+      if (f0 & 2) run_affect(L, 1, io.P.ccb_fn[0]);
+      else u_mod = false;
+    }
+  } else {
+    L.event_last = 0;
+  }
+#endif
+#if DEGPU_NDCB > 0
+  bool dsaved = false;
+#pragma unroll
+  for (int j = 0; j < DEGPU_NDCB; j++) {
+    const int fn = io.P.dcb_fn[j];
+    float x[N];
+#pragma unroll
+    for (int c = 0; c < N; c++) x[c] = L.u[c];
+    if (degpu_dcb_condition(fn, x, L.p, (Tt)TP::out(L.t))) {
+      save_values(L, io, i, save_every);
+      dsaved = true;
+      u_mod = true;
+      run_affect(L, 2, fn);
+    }
+  }
+  saved = dsaved;  // handle_callbacks! returns the discrete chain's saved_in_cb (:293-297)
+#endif
+  return saved;
+}
+#endif
+
 // One attempt of step!.  Returns true when the trajectory is finished.  After an accepted
 // step that does not finish the span, the next step is set up right away (uprev = u,
 // FSAL k1 / k1 = f(u) / Jacobian), so the attempt path itself carries no set-up branch;
@@ -857,6 +1116,9 @@ template <bool ADAPTIVE>
 DEGPU_DEV bool advance(Lane& L, const Io& io, int i) {
   const Time t = L.t;
   float unew[N], err[N];
+#if DEGPU_TSTOPS
+  bool at_tstop = false;
+#endif
   if (ADAPTIVE) {
     float dt = L.dtnew;
     if (dt < 1.0e-14f) { L.status = DEGPU_RET_DTLESSTHANMIN; return true; }
@@ -874,22 +1136,53 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, int i) {
       return false;
     }
     if (L.naccept == 0 && io.P.dt_first) io.P.dt_first[i] = dt;
+#if DEGPU_TSTOPS
+    // not snapped to tf: stop at the next tstop instead, u = integ(tstop) (:157-167)
+    if (!(TP::rem(L.tf, t, dt) < 1.0e-14f)) {
+      Time s;
+      if (tstop_due(L, io, t, dt, s)) { L.t = s; L.tstops_idx++; at_tstop = true; }
+    }
+#endif
   } else {
     if (++L.nattempt > io.P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
     float dt = L.dt;
     L.tprev = t;
-    L.t = TP::add(t, dt);
+#if DEGPU_TSTOPS
+    Time s;
+    if (tstop_due(L, io, t, dt, s)) {  // step to the tstop with dt = tstop - tprev (:16-22)
+      L.t = s;
+      dt = TP::rem(s, t, 0.0f);
+      L.tstops_idx++;
+    } else
+#endif
+      L.t = TP::add(t, dt);
     attempt<false>(L, t, dt, unew, err);
   }
 #pragma unroll
   for (int c = 0; c < N; c++) L.u[c] = unew[c];
+#if DEGPU_TSTOPS
+  if (at_tstop) {
+    float v[N];
+    interp(L, TP::theta(L.t, L.tprev, L.dt), L.dt, v);
+#pragma unroll
+    for (int c = 0; c < N; c++) L.u[c] = v[c];
+  }
+#endif
   L.naccept++;
-  save_values(L, io, i, !ADAPTIVE && io.P.save_everystep);
+  const bool save_every = !ADAPTIVE && io.P.save_everystep;
+#if DEGPU_CALLBACKS
+  bool u_mod = false;
+  if (!handle_callbacks<ADAPTIVE>(L, io, i, save_every, u_mod)) save_values(L, io, i, save_every);
+  const bool done = !TP::lt(L.t, L.tf) || L.status == DEGPU_RET_TERMINATED;
+#else
+  save_values(L, io, i, save_every);
   const bool done = !TP::lt(L.t, L.tf);
+  const bool u_mod = false;
+#endif
   if (!done) {
 #pragma unroll
     for (int c = 0; c < N; c++) L.uprev[c] = L.u[c];
-    begin_step(L, false);
+    begin_step(L, u_mod);
   }
   return done;
 }

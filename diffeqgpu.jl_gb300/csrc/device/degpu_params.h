@@ -47,7 +47,19 @@ typedef struct degpu_kparams {
   int chunk;              /* persistent driver: trajectories claimed per warp refill */
   int stage_cols;         /* saved rows staged per lane in shared memory (blockDim*L*N floats) */
   int shared_saveat;      /* shared saveat grid converted once per block into shared memory */
-  int pad_;
+  int ntstops;            /* 0 = no tstops */
+  const void* tstops;     /* [ntstops] Tt, ascending, shared by all trajectories */
+  /* callbacks (at most DEGPU_KP_MAX_CB of each kind): source function index, flags
+   * (bit 0 affect!, bit 1 affect_neg!, bits 2-3 root-find mode), repeat-event tolerance,
+   * repeat nudge and dt relaxation of each continuous callback; function index of each
+   * discrete callback */
+  int ccb_fn[8];
+  int ccb_flags[8];
+  float ccb_abstol[8];
+  float ccb_nudge[8];
+  float ccb_dtrelax[8];
+  int dcb_fn[8];
 } degpu_kparams;
+#define DEGPU_KP_MAX_CB 8
 
 #endif

@@ -209,3 +209,19 @@ using degpu::Dual;
 using degpu::dsin;
 using degpu::dcos;
 using degpu::dexp;
+
+// ------------------------------------------------------------------ callbacks (user side)
+// The affect functions of GPUContinuousCallback / GPUDiscreteCallback
+// (src/ensemblegpukernel/callbacks.jl) receive the fields of the integrator that the
+// reference's affects use: the state (modifiable in place), the parameters, the time, the
+// step, and terminate! (integrator_utils.jl:52-65).  degpu_time is the time type of the
+// solve (float for a Float32 tspan, double for FP64 time).
+typedef DEGPU_TT degpu_time;
+struct degpu_integrator {
+  float* u;
+  const float* p;
+  degpu_time t;
+  float dt;
+  int terminated;
+};
+__device__ __forceinline__ void degpu_terminate(degpu_integrator& I) { I.terminated = 1; }

@@ -30,7 +30,23 @@ class Options(ctypes.Structure):
         ("abstol", ctypes.c_double), ("reltol", ctypes.c_double), ("maxiters", ctypes.c_longlong),
         ("dt0", ctypes.c_void_p), ("tolscale", ctypes.c_void_p), ("seed", ctypes.c_ulonglong),
         ("traj_offset", ctypes.c_longlong), ("block", ctypes.c_int), ("chunk", ctypes.c_int),
+        ("ntstops", ctypes.c_int), ("tstops", ctypes.c_void_p), ("callbacks", ctypes.c_void_p),
     ]
+
+
+class ContinuousCallbackC(ctypes.Structure):
+    _fields_ = [("fn", ctypes.c_int), ("has_affect", ctypes.c_int), ("has_affect_neg", ctypes.c_int),
+                ("rootfind", ctypes.c_int), ("abstol", ctypes.c_double), ("repeat_nudge", ctypes.c_double),
+                ("dtrelax", ctypes.c_double)]
+
+
+class CallbacksC(ctypes.Structure):
+    _fields_ = [("n_continuous", ctypes.c_int), ("continuous", ctypes.POINTER(ContinuousCallbackC)),
+                ("n_discrete", ctypes.c_int), ("discrete", ctypes.POINTER(ctypes.c_int))]
+
+
+MAX_CALLBACKS = 8
+ROOTFIND_LEFT, ROOTFIND_RIGHT, ROOTFIND_NONE = 0, 1, 2
 
 
 class Outputs(ctypes.Structure):
@@ -51,6 +67,7 @@ class DegpuError(RuntimeError):
 _P = ctypes.c_void_p
 SIGNATURES = {
     "degpu_version": (ctypes.c_char_p, []),
+    "degpu_abi_struct_sizes": (None, [ctypes.POINTER(ctypes.c_int)] * 5),
     "degpu_last_error": (ctypes.c_char_p, []),
     "degpu_rhs_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
     "degpu_rhs_destroy": (None, [_P]),

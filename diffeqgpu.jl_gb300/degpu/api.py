@@ -285,6 +285,114 @@ def normalize_saveat(saveat, tspan, Tt, adaptive: bool):
     return np.asarray(saveat, dtype=np.float64).astype(Tt)
 
 
+# ---------------------------------------------------------------------- callbacks
+LeftRootFind, RightRootFind, NoRootFind = "LeftRootFind", "RightRootFind", "NoRootFind"
+_ROOTFIND = {LeftRootFind: _lib.ROOTFIND_LEFT, RightRootFind: _lib.ROOTFIND_RIGHT, NoRootFind: _lib.ROOTFIND_NONE}
+_SAVE_POS_MSG = ("Callback `save_positions` are incompatible with kernel-based GPU ODE solvers due requiring static "
+                 "sizing. Please ensure `save_positions = (false,false)` is set in all callback definitions used "
+                 "with such solvers.")
+
+
+class ContinuousCallback:
+    """GPUContinuousCallback (src/ensemblegpukernel/callbacks.jl:34-124).
+
+    The condition and affects are CUDA C functions of the ODEFunction's source,
+    `degpu_ccb_condition(fn, u, p, t)`, `degpu_ccb_affect(fn, I)` and
+    `degpu_ccb_affect_neg(fn, I)`; `fn` selects which one.  `affect=False` stands for
+    `affect! = nothing` and `affect_neg=False` for `affect_neg! = nothing`; by default
+    affect_neg! is present exactly when affect! is (`affect_neg! = affect!`).  abstol defaults
+    to 100 eps(Float32), the value a ContinuousCallback gets when converted for the kernels
+    (callbacks.jl:112-119)."""
+
+    default_abstol = 100 * float(np.finfo(np.float32).eps)
+
+    def __init__(self, fn: int = 0, affect: bool = True, affect_neg=None, *, rootfind=LeftRootFind,
+                 save_positions=(False, False), interp_points=10, dtrelax=1.0, abstol=None, reltol=0.0,
+                 repeat_nudge=0.01):
+        if tuple(save_positions) != (False, False):
+            raise ValueError(_SAVE_POS_MSG)
+        if rootfind not in _ROOTFIND:
+            raise ValueError(f"rootfind must be one of {list(_ROOTFIND)}")
+        self.fn = int(fn)
+        self.affect = bool(affect)
+        self.affect_neg = self.affect if affect_neg is None else bool(affect_neg)
+        self.rootfind = rootfind
+        self.save_positions = (False, False)
+        self.interp_points = interp_points
+        self.dtrelax = float(dtrelax)
+        self.abstol = self.default_abstol if abstol is None else float(abstol)
+        self.reltol = reltol
+        self.repeat_nudge = float(repeat_nudge)
+
+
+class GPUContinuousCallback(ContinuousCallback):
+    """The kernels' own constructor: abstol defaults to 10 eps(Float32) (callbacks.jl:94-103)."""
+    default_abstol = 10 * float(np.finfo(np.float32).eps)
+
+
+class DiscreteCallback:
+    """GPUDiscreteCallback (callbacks.jl:1-32): `degpu_dcb_condition(fn, u, p, t)` and
+    `degpu_dcb_affect(fn, I)` of the ODEFunction's source."""
+
+    def __init__(self, fn: int = 0, *, save_positions=(False, False)):
+        if tuple(save_positions) != (False, False):
+            raise ValueError(_SAVE_POS_MSG)
+        self.fn = int(fn)
+        self.save_positions = (False, False)
+
+
+GPUDiscreteCallback = DiscreteCallback
+
+
+class CallbackSet:
+    """CallbackSet(cb...): continuous and discrete members in order (nested sets flatten)."""
+
+    def __init__(self, *cbs):
+        self.continuous, self.discrete = [], []
+        for c in cbs:
+            if c is None:
+                continue
+            if isinstance(c, CallbackSet):
+                self.continuous += c.continuous
+                self.discrete += c.discrete
+            elif isinstance(c, ContinuousCallback):
+                self.continuous.append(c)
+            elif isinstance(c, DiscreteCallback):
+                self.discrete.append(c)
+            else:
+                raise TypeError(f"not a GPU callback: {c!r}")
+        if len(self.continuous) > _lib.MAX_CALLBACKS or len(self.discrete) > _lib.MAX_CALLBACKS:
+            raise ValueError(f"at most {_lib.MAX_CALLBACKS} continuous and {_lib.MAX_CALLBACKS} discrete callbacks")
+
+    def cstruct(self):
+        """(degpu_callbacks, keep-alive) for the C ABI."""
+        nc, nd = len(self.continuous), len(self.discrete)
+        carr = (_lib.ContinuousCallbackC * max(nc, 1))()
+        for j, c in enumerate(self.continuous):
+            carr[j] = _lib.ContinuousCallbackC(c.fn, int(c.affect), int(c.affect_neg), _ROOTFIND[c.rootfind],
+                                               c.abstol, c.repeat_nudge, c.dtrelax)
+        darr = (ctypes.c_int * max(nd, 1))(*[d.fn for d in self.discrete])
+        st = _lib.CallbacksC(nc, ctypes.cast(carr, ctypes.POINTER(_lib.ContinuousCallbackC)), nd,
+                             ctypes.cast(darr, ctypes.POINTER(ctypes.c_int)))
+        return st, (carr, darr)
+
+
+def as_callback_set(callback):
+    if callback is None:
+        return None
+    cs = callback if isinstance(callback, CallbackSet) else CallbackSet(callback)
+    return cs if (cs.continuous or cs.discrete) else None
+
+
+def tstops_extra_length(tspan, dt, tstops, Tt) -> int:
+    """length(tstops) - count(x -> x in tstops, t0:dt:tf) (lowerlevel_solve.jl:73-77)."""
+    t0, tf = float(Tt(tspan[0])), float(Tt(tspan[1]))
+    n = fixed_step_length(tspan, dt, Tt)
+    grid = np.asarray([Tt(t0 + k * float(Tt(dt))) for k in range(n)], dtype=Tt)
+    ts = np.asarray(tstops, dtype=Tt)
+    return int(ts.size - np.isin(grid, ts).sum())
+
+
 def fixed_step_length(tspan, dt, Tt) -> int:
     """length(tspan[1]:dt:tspan[2]) (lowerlevel_solve.jl:73)."""
     t0, tf, dt = float(Tt(tspan[0])), float(Tt(tspan[1])), float(Tt(dt))
@@ -347,7 +455,7 @@ def _torch_device(dev):
 
 def _options(alg, Tt, *, dt, abstol=1e-6, reltol=1e-3, save_everystep=False, saveat_dev=None, nsaveat=0,
              per_traj=False, mode="fast", driver="auto", maxiters=0, dt0=None, tolscale=None, seed=0,
-             traj_offset=0, block=0, chunk=0, jac="auto"):
+             traj_offset=0, block=0, chunk=0, jac="auto", tstops_dev=None, ntstops=0, callbacks_ptr=None):
     o = _lib.Options()
     o.alg = alg.alg_id
     o.time_type = _lib.TIME_F64 if Tt == np.float64 else _lib.TIME_F32
@@ -371,6 +479,9 @@ def _options(alg, Tt, *, dt, abstol=1e-6, reltol=1e-3, save_everystep=False, sav
     o.traj_offset = int(traj_offset)
     o.block = int(block)
     o.chunk = int(chunk)
+    o.ntstops = int(ntstops)
+    o.tstops = tstops_dev
+    o.callbacks = callbacks_ptr
     return o
 
 
@@ -385,7 +496,8 @@ class KernelResult:
 
 
 def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None, save_everystep=None,
-                  abstol=1e-6, reltol=1e-3, stream=None, stats=True, trace=False, **kw) -> KernelResult:
+                  abstol=1e-6, reltol=1e-3, stream=None, stats=True, trace=False, callback=None, tstops=None,
+                  **kw) -> KernelResult:
     import torch
     f = probs.f
     Tt = probs.Tt
@@ -411,6 +523,8 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
             if save_everystep:
                 L = fixed_step_length(tsp0, dt, Tt) if not adaptive else \
                     int(math.ceil(float(Tt(tsp0[1]) - Tt(tsp0[0])) / float(Tt(dt)))) + 1
+                if tstops is not None and not adaptive:
+                    L += tstops_extra_length(tsp0, dt, tstops, Tt)
             else:
                 L = 2
         else:
@@ -425,11 +539,21 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
     dtf = torch.zeros(B, dtype=torch.float32, device=dev) if trace else None
     dt0 = kw.pop("dt0", None)
     tolscale = kw.pop("tolscale", None)
+    ts_dev = None
+    if tstops is not None and np.size(tstops):
+        ts_dev = torch.as_tensor(np.sort(np.asarray(tstops, dtype=Tt).ravel()), device=dev)
+    cbs = as_callback_set(callback)
+    cb_struct = cb_keep = None
+    if cbs is not None:
+        cb_struct, cb_keep = cbs.cstruct()
     opt = _options(alg, Tt, dt=dt, abstol=abstol, reltol=reltol, save_everystep=save_everystep,
                    saveat_dev=None if sa_dev is None else sa_dev.data_ptr(),
                    nsaveat=0 if sa_dev is None else L, per_traj=per_traj,
                    dt0=None if dt0 is None else dt0.data_ptr(),
-                   tolscale=None if tolscale is None else tolscale.data_ptr(), **kw)
+                   tolscale=None if tolscale is None else tolscale.data_ptr(),
+                   tstops_dev=None if ts_dev is None else ts_dev.data_ptr(),
+                   ntstops=0 if ts_dev is None else ts_dev.numel(),
+                   callbacks_ptr=None if cb_struct is None else ctypes.addressof(cb_struct), **kw)
     out = _lib.Outputs(ts.data_ptr(), us.data_ptr(), L, rc.data_ptr(), None if na is None else na.data_ptr(),
                        None if nr is None else nr.data_ptr(), None if dtf is None else dtf.data_ptr())
     st = stream if stream is not None else torch.cuda.current_stream(dev)
@@ -448,9 +572,8 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
 def vectorized_solve(probs: DeviceProblems, prob: ODEProblem, alg, *, dt, saveat=None, save_everystep=True,
                      debug=False, callback=None, tstops=None, **kw):
     """Fixed-step batched solve (lowerlevel_solve.jl:53-131, 134-199).  Returns device (ts, us)."""
-    if callback is not None or tstops is not None:
-        raise NotImplementedError("callbacks and tstops are not supported by this engine yet")
-    r = _solve_device(probs, alg, False, dt=dt, saveat=saveat, save_everystep=save_everystep, **kw)
+    r = _solve_device(probs, alg, False, dt=dt, saveat=saveat, save_everystep=save_everystep, callback=callback,
+                      tstops=tstops, **kw)
     return r.ts, r.us
 
 
@@ -459,10 +582,8 @@ def vectorized_asolve(probs: DeviceProblems, prob: ODEProblem, alg, *, dt=0.1, s
     """Adaptive batched solve (lowerlevel_solve.jl:253-346).  Returns device (ts, us)."""
     if isinstance(alg, GPUSDEAlgorithm):
         raise NotImplementedError("Adaptive time-stepping is not supported yet with GPUEM.")
-    if callback is not None or tstops is not None:
-        raise NotImplementedError("callbacks and tstops are not supported by this engine yet")
     r = _solve_device(probs, alg, True, dt=dt, saveat=saveat, save_everystep=save_everystep,
-                      abstol=abstol, reltol=reltol, **kw)
+                      abstol=abstol, reltol=reltol, callback=callback, tstops=tstops, **kw)
     return r.ts, r.us
 
 
@@ -557,13 +678,11 @@ def _build_batch(ens: EnsembleProblem, I: range):
 
 def solve(ens: EnsembleProblem, alg, ensemblealg: EnsembleGPUKernel, *, trajectories: int, batch_size=None,
           adaptive: bool = True, dt=None, saveat=None, save_everystep=None, abstol=1.0e-6, reltol=1.0e-3,
-          callback=None, tstops=None, unstable_check=None, **kw) -> EnsembleSolution:
+          callback=None, tstops=None, unstable_check=None, merge_callbacks=True, **kw) -> EnsembleSolution:
     """SciMLBase.solve for EnsembleGPUKernel (src/solve.jl:1-165, 174-287, 382-419)."""
     import torch
     if not isinstance(ensemblealg, EnsembleGPUKernel):
         raise TypeError("ensemblealg must be EnsembleGPUKernel")
-    if callback is not None or tstops is not None:
-        raise NotImplementedError("callbacks and tstops are not supported by this engine yet")
     if isinstance(alg, GPUSDEAlgorithm) and adaptive:
         raise NotImplementedError("Adaptive EM is not supported yet.")
     if dt is None:
@@ -590,7 +709,7 @@ def solve(ens: EnsembleProblem, alg, ensemblealg: EnsembleGPUKernel, *, trajecto
         t0s.append(np.asarray(tsp)[:, 0])
         dp = DeviceProblems(prob.f, u0, p, tsp, Tt, dev, sa)
         r = _solve_device(dp, alg, adaptive, dt=dt, saveat=saveat, save_everystep=save_everystep,
-                          abstol=abstol, reltol=reltol, traj_offset=b0, **kw)
+                          abstol=abstol, reltol=reltol, traj_offset=b0, callback=callback, tstops=tstops, **kw)
         parts.append(r)
     torch.cuda.synchronize(dev)
     ts = np.concatenate([r.ts.cpu().numpy() for r in parts])

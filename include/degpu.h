@@ -68,6 +68,37 @@ extern "C" {
 typedef struct degpu_rhs_s degpu_rhs;
 typedef struct degpu_plan_s degpu_plan;
 
+/* ---- callbacks (src/ensemblegpukernel/callbacks.jl, integrators/integrator_utils.jl) ----
+ * The callback functions are CUDA C in the same source as the right-hand side:
+ *   continuous:  float degpu_ccb_condition(int fn, const float* u, const float* p, degpu_time t);
+ *                void  degpu_ccb_affect(int fn, degpu_integrator& I);
+ *                void  degpu_ccb_affect_neg(int fn, degpu_integrator& I);
+ *   discrete:    bool  degpu_dcb_condition(int fn, const float* u, const float* p, degpu_time t);
+ *                void  degpu_dcb_affect(int fn, degpu_integrator& I);
+ * degpu_time is float (DEGPU_TIME_F32) or double (DEGPU_TIME_F64); an affect may change
+ * I.u in place and call degpu_terminate(I) (terminate!, retcode Terminated).  Each member of
+ * a set names the function index fn it passes to those functions.  save_positions must be
+ * (false, false), as in the reference (callbacks.jl:13, 72). */
+#define DEGPU_MAX_CALLBACKS 8
+#define DEGPU_ROOTFIND_LEFT 0  /* SciMLBase.LeftRootFind (default) */
+#define DEGPU_ROOTFIND_RIGHT 1 /* SciMLBase.RightRootFind */
+#define DEGPU_ROOTFIND_NONE 2  /* SciMLBase.NoRootFind: the event is placed at the step end */
+typedef struct degpu_continuous_callback {
+  int fn;               /* function index passed to degpu_ccb_* */
+  int has_affect;       /* 0: affect! === nothing (upcrossings are ignored) */
+  int has_affect_neg;   /* 0: affect_neg! === nothing (downcrossings are ignored) */
+  int rootfind;         /* DEGPU_ROOTFIND_* */
+  double abstol;        /* repeat-event tolerance: 100 eps(Float32) when converted from a ContinuousCallback */
+  double repeat_nudge;  /* 1/100 */
+  double dtrelax;       /* 1 */
+} degpu_continuous_callback;
+typedef struct degpu_callbacks {
+  int n_continuous;                              /* <= DEGPU_MAX_CALLBACKS */
+  const degpu_continuous_callback* continuous;   /* host array [n_continuous] */
+  int n_discrete;                                /* <= DEGPU_MAX_CALLBACKS */
+  const int* discrete;                           /* host array [n_discrete]: function indices */
+} degpu_callbacks;
+
 /* The isbits ImmutableODEProblem array of the reference, flattened (device pointers). */
 typedef struct degpu_problems {
   const float* u0;    /* [B][N] */
@@ -97,6 +128,9 @@ typedef struct degpu_options {
   long long traj_offset;   /* global index of trajectory 0 (noise streams of shards) */
   int block;            /* threads per block (0 = autotuned/default) */
   int chunk;            /* persistent driver: trajectories per warp refill (0 = default) */
+  int ntstops;          /* tstops: 0 = none */
+  const void* tstops;   /* device [ntstops] of the time type, ascending, shared by all trajectories */
+  const degpu_callbacks* callbacks; /* NULL = no callbacks (CallbackSet(nothing)) */
 } degpu_options;
 
 /* outputs (caller-owned device buffers) */
@@ -111,6 +145,9 @@ typedef struct degpu_outputs {
 } degpu_outputs;
 
 const char* degpu_version(void);
+/* sizeof of the ABI structs (options, outputs, problems, continuous callback, callback set),
+ * so that bindings can check their mirrors of these layouts */
+void degpu_abi_struct_sizes(int* options, int* outputs, int* problems, int* continuous_callback, int* callbacks);
 /* last error message of the calling thread */
 const char* degpu_last_error(void);
 

@@ -57,7 +57,7 @@ enum { RET_DEFAULT = 0, RET_SUCCESS = 1, RET_TERMINATED = 2, RET_DTMIN = 3, RET_
 enum { JAC_AD = 0, JAC_ANALYTIC = 1, JAC_FINITEDIFF = 2 };
 enum {
   M_LORENZ = 0, M_ROBERTSON = 1, M_DECAY = 2, M_GROWTH = 3, M_LINEAR15 = 4,
-  M_GBM = 5, M_LORENZ_ADDNOISE = 6, M_OSC = 7
+  M_GBM = 5, M_LORENZ_ADDNOISE = 6, M_OSC = 7, M_BALL = 8
 };
 #define MAXN 16
 #define MAXP 8
@@ -91,7 +91,8 @@ template <int NP> static inline Dual<NP> operator-(Dual<NP> b, float a) { Dual<N
  *   linear15   test/gpu_kernel_de/stiff_ode/gpu_ode_regression.jl:24-26 (u' = 1.01 u, N=15)
  *   gbm        test/gpu_kernel_de/gpu_sde_convergence.jl:6-8           (f = p1 u, g = p2 u)
  *   lorenz+additive noise  test/gpu_kernel_de/gpu_sde_regression.jl:47-58
- *   osc        harmonic oscillator u1' = u2, u2' = -p1^2 u1 (non-chaotic known answer) */
+ *   osc        harmonic oscillator u1' = u2, u2' = -p1^2 u1 (non-chaotic known answer)
+ *   ball       bouncing ball u1' = u2, u2' = -p1 (test/gpu_kernel_de/gpu_ode_continuous_callbacks.jl:6-10) */
 struct ModelInfo { int N, P, has_jac, has_tgrad, is_sde; };
 static ModelInfo model_info(int m) {
   switch (m) {
@@ -103,6 +104,7 @@ static ModelInfo model_info(int m) {
     case M_GBM: return {1, 2, 0, 0, 1};
     case M_LORENZ_ADDNOISE: return {3, 3, 0, 0, 1};
     case M_OSC: return {2, 1, 1, 1, 0};
+    case M_BALL: return {2, 1, 0, 0, 0};
   }
   return {0, 0, 0, 0, 0};
 }
@@ -127,6 +129,7 @@ static void model_f(int m, S* du, const S* u, const float* p, float t) {
     case M_LINEAR15: for (int i = 0; i < 15; i++) du[i] = 1.01f * u[i]; break;
     case M_GBM: du[0] = p[0] * u[0]; break;
     case M_OSC: { du[0] = u[1]; du[1] = -(p[0] * p[0]) * u[0]; } break;
+    case M_BALL: { du[0] = u[1]; du[1] = S(-p[0]); } break;
   }
 }
 
@@ -149,6 +152,37 @@ static void model_jac(int m, float* J, const float* u, const float* p, float t) 
   }
 }
 static void model_tgrad(int m, float* dT, int N) { (void)m; for (int i = 0; i < N; i++) dT[i] = 0.0f; }
+
+/* callbacks of the models that define them, with the expressions of their CUDA C sources
+ *   ball   continuous fn 0: condition u1, affect! = affect_neg! : u += (0, -2) .* u
+ *                         (gpu_ode_continuous_callbacks.jl:18-24); fn 1: terminate! at contact
+ *   decay  discrete fn 0: t == 2.4, fn 1: t == 4.0 (u += 10; gpu_ode_discrete_callbacks.jl:16-22
+ *          with tstops at those times); fn 2: terminate! once u < 1 */
+struct CbInteg { float* u; const float* p; double t; float dt; int terminated; };
+static float model_ccb_condition(int m, int fn, const float* u, const float* p, double t) {
+  (void)fn; (void)p; (void)t;
+  if (m == M_BALL) return u[0];
+  return 0.0f;
+}
+static void model_ccb_affect(int m, int fn, CbInteg& I) {
+  if (m == M_BALL) {
+    if (fn == 1) { I.terminated = 1; return; }
+    I.u[0] = I.u[0] + 0.0f * I.u[0];
+    I.u[1] = I.u[1] + -2.0f * I.u[1];
+  }
+}
+static int model_dcb_condition(int m, int fn, const float* u, const float* p, double t) {
+  (void)p;
+  if (m != M_DECAY) return 0;
+  if (fn == 0) return (float)t == 2.4f;
+  if (fn == 1) return (float)t == 4.0f;
+  return u[0] < 1.0f;
+}
+static void model_dcb_affect(int m, int fn, CbInteg& I) {
+  if (m != M_DECAY) return;
+  if (fn == 2) { I.terminated = 1; return; }
+  I.u[0] = I.u[0] + 10.0f;
+}
 
 /* SDE noise g (diagonal) */
 static void model_g(int m, float* g, const float* u, const float* p) {
@@ -315,6 +349,14 @@ typedef struct {
   unsigned long long seed; /* EM: key of the counter-based generator */
   const float* dt0;    /* optional per-trajectory initial dt (overrides dt) */
   const float* tolscale; /* optional per-trajectory multiplier of abstol and reltol */
+  int ntstops;         /* tstops (ascending, shared by all trajectories) */
+  const double* tstops;
+  int nccb;            /* continuous callbacks: function index, flags (bit 0 affect!, bit 1
+                        * affect_neg!, bits 2-3 root-find mode), abstol, repeat nudge, dtrelax */
+  int ccb_fn[8], ccb_flags[8];
+  float ccb_abstol[8], ccb_nudge[8], ccb_dtrelax[8];
+  int ndcb;            /* discrete callbacks: function index */
+  int dcb_fn[8];
 } oracle_cfg;
 }
 
@@ -332,6 +374,9 @@ template <class Tt> struct Integ {
   int cur_t, step_idx;
   int retcode;
   long long nattempt, naccept, nreject;
+  int tstops_idx;          /* next tstop, 0-based */
+  int event_last;          /* event_last_time (1-based callback index, 0 = none) */
+  float last_event_error;  /* condition residual at the last located event */
 };
 
 /* time argument handed to f: `t + c*dt` in Tt, passed to the FP32 right-hand side */
@@ -666,6 +711,202 @@ static void interpolate(int m, int alg, const Integ<Tt>& ig, const float* p, flo
   }
 }
 
+/* ------------------------------------------------------------------ callbacks (integrator_utils.jl:52-479)
+ * Julia's sign / eps / nextfloat / max on the time type, the ITP root finder, event location
+ * and application.  To is the time type at the boundary (float, or double for the pair time). */
+static inline float jl_sign(float x) { return (x == 0.0f || x != x) ? x : copysignf(1.0f, x); }
+static inline float o_abs(float x) { return fabsf(x); }
+static inline double o_abs(double x) { return fabs(x); }
+static inline float o_copysign(float a, float b) { return copysignf(a, b); }
+static inline double o_copysign(double a, double b) { return copysign(a, b); }
+template <class To> static inline To o_max(To x, To y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
+static inline float o_eps(float x) { /* ldexp(eps(Float32), exponent(x)); nextfloat(0) below floatmin */
+  uint32_t b; memcpy(&b, &x, 4);
+  uint32_t e = (b >> 23) & 0xffu, r;
+  if (e == 0xffu) r = 0x7fc00000u;
+  else if (e > 23u) r = (e - 23u) << 23;
+  else r = e == 0u ? 1u : (1u << (e - 1u));
+  float y; memcpy(&y, &r, 4); return y;
+}
+static inline double o_eps(double x) {
+  uint64_t b; memcpy(&b, &x, 8);
+  uint64_t e = (b >> 52) & 0x7ffull, r;
+  if (e == 0x7ffull) r = 0x7ff8000000000000ull;
+  else if (e > 52ull) r = (e - 52ull) << 52;
+  else r = e == 0ull ? 1ull : (1ull << (e - 1ull));
+  double y; memcpy(&y, &r, 8); return y;
+}
+static inline float o_nextfloat(float x) {
+  if (x != x || x == INFINITY) return x;
+  uint32_t b;
+  if (x == 0.0f) b = 1u; else { memcpy(&b, &x, 4); b = x > 0.0f ? b + 1u : b - 1u; }
+  float y; memcpy(&y, &b, 4); return y;
+}
+static inline double o_nextfloat(double x) {
+  if (x != x || x == (double)INFINITY) return x;
+  uint64_t b;
+  if (x == 0.0) b = 1ull; else { memcpy(&b, &x, 8); b = x > 0.0 ? b + 1ull : b - 1ull; }
+  double y; memcpy(&y, &b, 8); return y;
+}
+
+/* get_condition (integrator_utils.jl:461-479): u at t, uprev at tprev, else integ(abst) */
+template <class Tt>
+static float cond_at(int m, int alg, const Integ<Tt>& ig, const float* p, int fn, typename TOut<Tt>::T abst) {
+  typedef typename TOut<Tt>::T To;
+  float x[MAXN];
+  if (abst == (To)t_out(ig.t)) for (int c = 0; c < ig.N; c++) x[c] = ig.u[c];
+  else if (abst == (To)t_out(ig.tprev)) for (int c = 0; c < ig.N; c++) x[c] = ig.uprev[c];
+  else interpolate(m, alg, ig, p, t_theta(t_from<Tt>((double)abst), ig.tprev, ig.dt), ig.dt, x);
+  return model_ccb_condition(m, fn, x, p, (double)abst);
+}
+
+/* gpu_find_root (integrator_utils.jl:302-355): ITP, scaled_k1 = 0.2, k2 = 2, n0 = 10 */
+template <class Tt>
+static typename TOut<Tt>::T itp_root(int m, int alg, const Integ<Tt>& ig, const float* p, int fn,
+                                     typename TOut<Tt>::T left, typename TOut<Tt>::T right, int rootfind) {
+  typedef typename TOut<Tt>::T To;
+  float fl = cond_at(m, alg, ig, p, fn, left), fr = cond_at(m, alg, ig, p, fn, right);
+  const To span0 = right - left;
+  const To k1 = (To)0.2 / span0;
+  To eps_s = span0 * (To)512;
+  for (int it = 0; it < 100; it++) {
+    const To span = right - left;
+    const To mid = (left + right) / (To)2;
+    const To r = eps_s - span / (To)2;
+    const To x_f = left + (span * (To)fl) / (To)(fl - fr);
+    const To delta = o_max<To>(k1 * span * span, o_eps(x_f));
+    const To diff = mid - x_f;
+    const To xt = (delta <= o_abs(diff)) ? x_f + o_copysign(delta, diff) : mid;
+    const To xp = (o_abs(xt - mid) <= r) ? xt : mid - o_copysign(r, diff);
+    const float yp = cond_at(m, alg, ig, p, fn, xp);
+    const float yps = yp * jl_sign(fr);
+    if (yps > 0.0f) { right = xp; fr = yp; }
+    else if (yps < 0.0f) { left = xp; fl = yp; }
+    else { left = xp; right = xp; break; }
+    eps_s = eps_s / (To)2;
+    if (o_nextfloat(left) >= right) break;
+  }
+  return rootfind == 1 ? right : left;
+}
+
+/* savevalues! (integrator_utils.jl:13-50) */
+template <class Tt>
+static void save_values(int m, int alg, Integ<Tt>& ig, const float* p, const double* sa, int nsa, int L,
+                        int save_every, typename TOut<Tt>::T* ts, float* us) {
+  const int N = ig.N;
+  if (!sa && save_every) {
+    if (ig.step_idx >= 0 && ig.step_idx < L) {
+      for (int i = 0; i < N; i++) us[(size_t)ig.step_idx * N + i] = ig.u[i];
+      ts[ig.step_idx] = t_out(ig.t);
+    }
+    ig.step_idx++;
+  } else if (sa) {
+    while (ig.cur_t < nsa && t_le(t_from<Tt>(sa[ig.cur_t]), ig.t)) {
+      Tt savet = t_from<Tt>(sa[ig.cur_t]);
+      float th = t_theta(savet, ig.tprev, ig.dt);
+      if (ig.cur_t < L) {
+        interpolate(m, alg, ig, p, th, ig.dt, us + (size_t)ig.cur_t * N);
+        ts[ig.cur_t] = (typename TOut<Tt>::T)sa[ig.cur_t];
+      }
+      ig.cur_t++;
+    }
+  }
+}
+
+template <class Tt>
+static void run_affect(int m, Integ<Tt>& ig, const float* p, int kind, int fn) {
+  CbInteg I{ig.u, p, (double)t_out(ig.t), ig.dt, 0};
+  if (kind == 2) model_dcb_affect(m, fn, I);
+  else model_ccb_affect(m, fn, I);  /* the built-in models use affect! as affect_neg! */
+  if (I.terminated) ig.retcode = RET_TERMINATED;
+}
+
+/* handle_callbacks! (:258-300) with find_callback_time (:357-428), apply_callback! (:212-256),
+ * change_t_via_interpolation! (:180-209) and apply_discrete_callback! (:67-150).
+ * Returns saved_in_cb. */
+template <class Tt>
+static int handle_callbacks(int m, const oracle_cfg* cfg, Integ<Tt>& ig, const float* p, const double* sa,
+                            int nsa, int L, int save_every, typename TOut<Tt>::T* ts, float* us) {
+  typedef typename TOut<Tt>::T To;
+  const int alg = cfg->alg, N = ig.N;
+  int saved = 0;
+  if (cfg->nccb > 0) {
+    int occ_best = 0, idx = 0;
+    To t_best = 0;
+    float sign_best = 0.0f, res_best = 0.0f;
+    for (int j = 0; j < cfg->nccb; j++) {
+      const int fn = cfg->ccb_fn[j], fl = cfg->ccb_flags[j];
+      To bottom_t = (To)t_out(ig.tprev);
+      float bottom_c = model_ccb_condition(m, fn, ig.uprev, p, (double)bottom_t);
+      if (ig.event_last == j + 1 && fabsf(bottom_c - ig.last_event_error) <= cfg->ccb_abstol[j]) {
+        bottom_t = bottom_t + (To)(ig.dt * cfg->ccb_nudge[j]);
+        bottom_c = cond_at(m, alg, ig, p, fn, bottom_t);
+      }
+      const float bs = jl_sign(bottom_c);
+      const To top_t = (To)t_out(ig.t);
+      const float tsg = jl_sign(cond_at(m, alg, ig, p, fn, top_t));
+      const int occ = ((bs < 0.0f && (fl & 1)) || (bs > 0.0f && (fl & 2))) && bs * tsg <= 0.0f;
+      To te = top_t;
+      float res = 0.0f;
+      const int rootfind = (fl >> 2) & 3;
+      if (occ && rootfind != 2 && tsg != 0.0f) {
+        te = itp_root(m, alg, ig, p, fn, bottom_t, top_t, rootfind);
+        res = cond_at(m, alg, ig, p, fn, te);
+      }
+      if (occ && (!occ_best || te < t_best)) { occ_best = 1; t_best = te; sign_best = bs; res_best = res; idx = j + 1; }
+    }
+    if (occ_best) {
+      ig.event_last = idx;
+      ig.last_event_error = res_best;
+      const To tcur = (To)t_out(ig.t);
+      if (t_best != tcur) {
+        float v[MAXN];
+        interpolate(m, alg, ig, p, t_theta(t_from<Tt>((double)t_best), ig.tprev, ig.dt), ig.dt, v);
+        for (int c = 0; c < N; c++) ig.u[c] = v[c];
+        To q = (tcur - t_best) / (To)ig.dt;
+        ig.step_idx -= (int)(sizeof(To) == 8 ? rint((double)q) : rintf((float)q));
+        ig.t = t_from<Tt>((double)t_best);
+      }
+      if (cfg->adaptive && ig.dtnew < 1.0e-12f) {
+        const To remaining = o_abs((To)t_out(ig.tf) - (To)t_out(ig.t));
+        const To relaxed = (To)(cfg->ccb_dtrelax[0] * ig.dt);
+        ig.dtnew = (float)((remaining < relaxed) ? remaining : relaxed);
+      }
+      save_values(m, alg, ig, p, sa, nsa, L, save_every, ts, us);
+      saved = 1;
+      ig.u_modified = 1;
+      const int f0 = cfg->ccb_flags[0];
+      if (sign_best < 0.0f) { if (f0 & 1) run_affect(m, ig, p, 0, cfg->ccb_fn[0]); else ig.u_modified = 0; }
+      else if (sign_best > 0.0f) { if (f0 & 2) run_affect(m, ig, p, 1, cfg->ccb_fn[0]); else ig.u_modified = 0; }
+    } else {
+      ig.event_last = 0;
+    }
+  }
+  if (cfg->ndcb > 0) {
+    int dsaved = 0;
+    for (int j = 0; j < cfg->ndcb; j++) {
+      const int fn = cfg->dcb_fn[j];
+      if (model_dcb_condition(m, fn, ig.u, p, (double)t_out(ig.t))) {
+        save_values(m, alg, ig, p, sa, nsa, L, save_every, ts, us);
+        dsaved = 1;
+        ig.u_modified = 1;
+        run_affect(m, ig, p, 2, fn);
+      }
+    }
+    saved = dsaved;
+  }
+  return saved;
+}
+
+/* `tstops[idx] - t - dt - 100 eps(T) < 0` (gpu_tsit5_perform_step.jl:18-19, :158-160) */
+template <class Tt>
+static int tstop_due(const oracle_cfg* cfg, const Integ<Tt>& ig, Tt t, float dt, Tt* s) {
+  if (ig.tstops_idx >= cfg->ntstops) return 0;
+  const float tol = sizeof(typename TOut<Tt>::T) == 8 ? (float)(100.0 * 2.220446049250313e-16) : 100.0f * 1.1920928955078125e-07f;
+  *s = t_from<Tt>(cfg->tstops[ig.tstops_idx]);
+  return t_rem(*s, t, dt) - tol < 0.0f;
+}
+
 /* ------------------------------------------------------------------ one trajectory (kernels.jl) */
 template <class Tt>
 static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* u0, const float* p, const double* tsp,
@@ -684,6 +925,7 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
   float tsc = cfg->tolscale ? cfg->tolscale[idx] : 1.0f;
   ig.abstol = cfg->abstol * tsc; ig.reltol = cfg->reltol * tsc;
   ig.u_modified = 1; ig.retcode = RET_DEFAULT;
+  ig.tstops_idx = 0; ig.event_last = 1; ig.last_event_error = 0.0f; /* stiff/types.jl:44-46 */
   Ctrl C = make_ctrl(alg_order(alg));
   ig.qold = C.qoldinit;
 
@@ -711,7 +953,9 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
       if (++ig.nattempt > cfg->maxiters) { ig.retcode = RET_MAXITERS; break; }
       float dt = ig.dt;
       ig.tprev = t;
-      ig.t = t_add(t, dt);
+      Tt tstop;
+      if (tstop_due(cfg, ig, t, dt, &tstop)) { ig.t = tstop; dt = t_rem(tstop, t, 0.0f); ig.tstops_idx++; }
+      else ig.t = t_add(t, dt);
       float u[MAXN];
       if (alg == ALG_TSIT5) {
         float k1[MAXN];
@@ -765,6 +1009,15 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
           int ns = alg == ALG_TSIT5 ? 7 : alg == ALG_VERN7 ? 10 : alg == ALG_RB23 ? 2 : 3;
           for (int s = 0; s < ns; s++) for (int i = 0; i < N; i++) ig.k[s][i] = kk[s][i];
           for (int i = 0; i < N; i++) ig.u[i] = u[i];
+          /* not snapped to tf: stop at the next tstop, u = integ(tstop) (:157-167) */
+          Tt tstop;
+          if (!(t_rem(ig.tf, t, dt) < 1.0e-14f) && tstop_due(cfg, ig, t, dt, &tstop)) {
+            ig.t = tstop;
+            ig.tstops_idx++;
+            float v[MAXN];
+            interpolate(m, alg, ig, p, t_theta(ig.t, ig.tprev, ig.dt), ig.dt, v);
+            for (int i = 0; i < N; i++) ig.u[i] = v[i];
+          }
           ig.naccept++;
         } else {
           ig.nreject++;
@@ -772,18 +1025,10 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
       }
       if (ig.retcode == RET_DTMIN || ig.retcode == RET_MAXITERS) break;
     }
-    /* ---------------- savevalues! (integrator_utils.jl:13-50) ---------------- */
-    if (!sa && save_every) {
-      if (ig.step_idx < L) { for (int i = 0; i < N; i++) US(ig.step_idx)[i] = ig.u[i]; ts[ig.step_idx] = t_out(ig.t); }
-      ig.step_idx++;
-    } else if (sa) {
-      while (ig.cur_t < nsa && t_le(SA(ig.cur_t), ig.t)) {
-        Tt savet = SA(ig.cur_t);
-        float th = t_theta(savet, ig.tprev, ig.dt);
-        if (ig.cur_t < L) { interpolate(m, alg, ig, p, th, ig.dt, US(ig.cur_t)); ts[ig.cur_t] = (Out)sa[ig.cur_t]; }
-        ig.cur_t++;
-      }
-    }
+    /* ---------------- callbacks, then savevalues! unless a callback saved (kernels.jl:50-51) */
+    int saved_in_cb = 0;
+    if (cfg->nccb > 0 || cfg->ndcb > 0) saved_in_cb = handle_callbacks(m, cfg, ig, p, sa, nsa, L, save_every, ts, us);
+    if (!saved_in_cb) save_values(m, alg, ig, p, sa, nsa, L, save_every, ts, us);
   }
   /* kernels.jl:53-62 / :133-142 */
   if (t_lt(tf, ig.t) && !sa) {

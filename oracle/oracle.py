@@ -17,7 +17,7 @@ LIB_PATH = HERE / "_build" / "liboracle.so"
 
 ALG = {"tsit5": 0, "vern7": 1, "rosenbrock23": 2, "rodas5p": 3, "em": 4}
 MODEL = {"lorenz": 0, "robertson": 1, "decay": 2, "growth": 3, "linear15": 4,
-         "gbm": 5, "lorenz_addnoise": 6, "osc": 7}
+         "gbm": 5, "lorenz_addnoise": 6, "osc": 7, "ball": 8}
 JAC = {"ad": 0, "analytic": 1, "finitediff": 2}
 RET = {"default": 0, "success": 1, "terminated": 2, "dtmin": 3, "maxiters": 4, "unstable": 5}
 
@@ -31,6 +31,10 @@ class OracleCfg(ctypes.Structure):
         ("abstol", ctypes.c_float), ("reltol", ctypes.c_float), ("maxiters", ctypes.c_longlong),
         ("seed", ctypes.c_ulonglong), ("dt0", ctypes.POINTER(ctypes.c_float)),
         ("tolscale", ctypes.POINTER(ctypes.c_float)),
+        ("ntstops", ctypes.c_int), ("tstops", ctypes.POINTER(ctypes.c_double)),
+        ("nccb", ctypes.c_int), ("ccb_fn", ctypes.c_int * 8), ("ccb_flags", ctypes.c_int * 8),
+        ("ccb_abstol", ctypes.c_float * 8), ("ccb_nudge", ctypes.c_float * 8), ("ccb_dtrelax", ctypes.c_float * 8),
+        ("ndcb", ctypes.c_int), ("dcb_fn", ctypes.c_int * 8),
     ]
 
 
@@ -88,8 +92,13 @@ def _ptr(a):
 
 def solve(model: str, alg: str, u0, p, tspan, *, adaptive: bool, dt: float, L: int,
           saveat=None, save_everystep=False, abstol=1e-6, reltol=1e-3, time_f64=False,
-          jac="ad", maxiters=10**7, seed=0, dt0=None, tolscale=None, nthreads=0):
+          jac="ad", maxiters=10**7, seed=0, dt0=None, tolscale=None, nthreads=0, tstops=None, ccb=(),
+          dcb=()):
     """Run the oracle ensemble.  u0 [B,N] f32, p [B,P] f32, tspan [B,2] f64 (or [2]).
+
+    tstops: shared ascending stop times; ccb: continuous callbacks as tuples
+    (fn, has_affect, has_affect_neg, rootfind 0 left / 1 right / 2 none, abstol, repeat_nudge,
+    dtrelax); dcb: discrete callback function indices.
 
     Returns (ts [B,L] (f32|f64), us [B,L,N] f32, retcode [B] i8, naccept [B] i32, nreject [B] i32).
     """
@@ -126,6 +135,23 @@ def solve(model: str, alg: str, u0, p, tspan, *, adaptive: bool, dt: float, L: i
     if tolscale is not None:
         ts_ = np.ascontiguousarray(tolscale, dtype=np.float32)
         cfg.tolscale = ts_.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    tst = None
+    if tstops is not None and np.size(tstops):
+        tst = np.ascontiguousarray(np.sort(np.asarray(tstops, dtype=np.float64).ravel()))
+        cfg.ntstops = tst.size
+        cfg.tstops = tst.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    if len(ccb) > 8 or len(dcb) > 8:
+        raise ValueError("at most 8 callbacks of each kind")
+    cfg.nccb = len(ccb)
+    for j, (fn, aff, neg, rf, atol, nudge, relax) in enumerate(ccb):
+        cfg.ccb_fn[j] = fn
+        cfg.ccb_flags[j] = (1 if aff else 0) | (2 if neg else 0) | (int(rf) << 2)
+        cfg.ccb_abstol[j] = atol
+        cfg.ccb_nudge[j] = nudge
+        cfg.ccb_dtrelax[j] = relax
+    cfg.ndcb = len(dcb)
+    for j, fn in enumerate(dcb):
+        cfg.dcb_fn[j] = fn
     ts = np.zeros((B, L), dtype=np.float64 if time_f64 else np.float32)
     us = np.zeros((B, L, N), dtype=np.float32)
     rc = np.zeros(B, dtype=np.int8)

@@ -27,10 +27,52 @@ def test_library_exports_every_header_symbol(degpu_mod):
     assert set(syms) <= set(_lib.SIGNATURES), set(syms) - set(_lib.SIGNATURES)
 
 
+def test_struct_layouts_match_the_library(degpu_mod):
+    """The ctypes mirrors of the ABI structs have the library's sizes."""
+    from degpu import _lib
+    v = [ctypes.c_int() for _ in range(5)]
+    degpu_mod.lib().degpu_abi_struct_sizes(*[ctypes.byref(x) for x in v])
+    mine = [_lib.Options, _lib.Outputs, _lib.Problems, _lib.ContinuousCallbackC, _lib.CallbacksC]
+    assert [x.value for x in v] == [ctypes.sizeof(t) for t in mine]
+
+
+def test_nvrtc_compiles_callback_kernels(degpu_mod):
+    """Kernels with tstops and continuous / discrete callback sets compile for every
+    algorithm (bouncing ball, decay with discrete events)."""
+    from degpu import _lib
+    n = ctypes.c_longlong()
+    for model, cs in (("ball", degpu_mod.CallbackSet(degpu_mod.ContinuousCallback(0), degpu_mod.ContinuousCallback(1))),
+                      ("decay", degpu_mod.CallbackSet(degpu_mod.DiscreteCallback(0), degpu_mod.DiscreteCallback(2)))):
+        f = degpu_mod.ODEFunction.builtin(model)
+        st, keep = cs.cstruct()
+        for alg in ("GPUTsit5", "GPUVern7", "GPURosenbrock23", "GPURodas5P"):
+            for adaptive in (0, 1):
+                o = _opts(degpu_mod, getattr(degpu_mod, alg)(), tt=np.float32, mode="parity")
+                o.callbacks = ctypes.addressof(st)
+                _lib.check(degpu_mod.lib().degpu_rhs_check(f.handle(), ctypes.byref(o), adaptive, ctypes.byref(n)))
+                assert n.value > 10_000
+
+
+def test_callback_validation(degpu_mod):
+    from degpu import _lib
+    f = degpu_mod.ODEFunction.builtin("ball")
+    bad = _lib.ContinuousCallbackC(0, 1, 1, 7, 1e-5, 0.01, 1.0)  # rootfind 7
+    st = _lib.CallbacksC(1, ctypes.pointer(bad), 0, None)
+    o = _opts(degpu_mod, degpu_mod.GPUTsit5())
+    o.callbacks = ctypes.addressof(st)
+    n = ctypes.c_longlong()
+    assert degpu_mod.lib().degpu_rhs_check(f.handle(), ctypes.byref(o), 1, ctypes.byref(n)) == -1
+    assert b"continuous callback" in degpu_mod.lib().degpu_last_error()
+    o = _opts(degpu_mod, degpu_mod.GPUTsit5())
+    o.ntstops = 3  # no pointer
+    assert degpu_mod.lib().degpu_rhs_check(f.handle(), ctypes.byref(o), 1, ctypes.byref(n)) == -1
+
+
 def test_version_and_builtins(degpu_mod):
     assert degpu_mod.lib().degpu_version() == b"0.1.0"
     for name, (n, p) in {"lorenz": (3, 3), "robertson": (3, 3), "decay": (1, 1), "growth": (1, 1),
-                         "linear15": (15, 1), "gbm": (1, 2), "lorenz_addnoise": (3, 3), "osc": (2, 1)}.items():
+                         "linear15": (15, 1), "gbm": (1, 2), "lorenz_addnoise": (3, 3), "osc": (2, 1),
+                         "ball": (2, 1)}.items():
         f = degpu_mod.ODEFunction.builtin(name)
         assert (f.nstate, f.nparam) == (n, p)
     with pytest.raises(KeyError):
