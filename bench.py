@@ -177,7 +177,8 @@ def oracle_error(us_final, idx, oref):
 def extra_configs(args, dev, flush):
     """Device-timed throughput of the other workloads (seeded synthetic inputs), each with
     its oracle error: fixed-step Lorenz (10,000), stiff Robertson (262,144; RB23 and
-    Rodas5P), and the uneven Lorenz batch (4,194,304; persistent vs one-per-thread)."""
+    Rodas5P), the uneven Lorenz batch (4,194,304; persistent vs one-per-thread), and
+    1,048,576 bouncing balls with a continuous callback."""
     import torch
 
     import degpu
@@ -254,6 +255,37 @@ def extra_configs(args, dev, flush):
                      "attempts_per_traj_mean": float((na + nr).mean()), "attempts_per_traj_max": int((na + nr).max())}
     out3["persistent_speedup"] = out3["persistent"]["trajectories_per_s"] / out3["naive"]["trajectories_per_s"]
     res[f"uneven_lorenz_{B3}"] = out3
+
+    # bouncing balls with a continuous callback (ITP event location + affect): heights
+    # U(5, 50), gravities U(5, 15), tspan (0, 12), 25 saved points, error against the exact bounce
+    B4 = 1 << 20
+    h4 = rng.uniform(5.0, 50.0, B4).astype(np.float32)
+    g4 = rng.uniform(5.0, 15.0, B4).astype(np.float32)
+    u04 = np.stack([h4, np.zeros(B4, np.float32)], 1)
+    sa4 = np.linspace(0.0, 12.0, 25)
+    fb = degpu.ODEFunction.builtin("ball")
+    pr4 = degpu.DeviceProblems(fb, u04, g4[:, None], np.tile([0.0, 12.0], (B4, 1)), np.float64, dev)
+    cb4 = degpu.ContinuousCallback(0)
+
+    def run4():
+        holder["r"] = degpu.api._solve_device(pr4, degpu.GPUTsit5(), True, dt=0.01, saveat=sa4, abstol=1e-7,
+                                              reltol=1e-7, callback=cb4)
+    ms = time_solve(run4)
+    r = holder["r"]
+    idx4 = np.arange(0, B4, B4 // 512)
+    us4 = r.us.cpu().numpy()[idx4]
+    T = np.sqrt(2 * h4[idx4].astype(np.float64) / g4[idx4])[:, None]
+    tt = sa4[None, :]
+    s4 = np.where(tt < T, tt, (tt - T) % (2 * T))
+    v0 = np.where(tt < T, 0.0, g4[idx4, None] * T)
+    hgt = np.where(tt < T, h4[idx4, None] - 0.5 * g4[idx4, None] * tt * tt, v0 * s4 - 0.5 * g4[idx4, None] * s4 * s4)
+    herr = np.abs(us4[:, :, 0] - hgt) / h4[idx4, None]
+    na, nr = r.naccept.cpu().numpy(), r.nreject.cpu().numpy()
+    res["bouncing_ball_callback_1M"] = {
+        "trajectories_per_s": B4 / (ms * 1e-3), "ms": ms, "attempts_per_traj": float((na + nr).mean()),
+        "height_rel_err_max": float(herr.max()), "height_rel_err_median": float(np.median(herr)),
+        "error_reference": "exact elastic bounce (analytic), 512 sampled trajectories x 25 saved points",
+        "retcodes_ok": bool((r.retcode.cpu().numpy() == 1).all())}
     return res
 
 

@@ -42,6 +42,28 @@ Base.@kwdef mutable struct Options
     traj_offset::Clonglong = 0
     block::Cint = 0
     chunk::Cint = 0
+    ntstops::Cint = 0
+    tstops::Ptr{Cvoid} = C_NULL          # CuArray of the time type (the `tstops` kwarg)
+    callbacks::Ptr{Cvoid} = C_NULL       # Ref{Callbacks}, see below
+end
+
+# GPUContinuousCallback fields the kernels use (callbacks.jl:34-124); the condition and
+# affects are the CUDA C functions degpu_ccb_* of the right-hand side's source, chosen by fn.
+struct ContinuousCallbackC
+    fn::Cint
+    has_affect::Cint
+    has_affect_neg::Cint
+    rootfind::Cint                       # 0 LeftRootFind, 1 RightRootFind, 2 NoRootFind
+    abstol::Cdouble
+    repeat_nudge::Cdouble
+    dtrelax::Cdouble
+end
+
+struct Callbacks
+    n_continuous::Cint
+    continuous::Ptr{ContinuousCallbackC}
+    n_discrete::Cint
+    discrete::Ptr{Cint}                  # degpu_dcb_* function index of each GPUDiscreteCallback
 end
 
 struct Outputs
