@@ -7,8 +7,9 @@ GPUTsit5 adaptive, reltol 1e-6, abstol 1e-8, initial dt 0.1, FP32 state with FP6
 seeded synthetic inputs.  A step is one full ensemble solve (one CUDA-graph launch of the
 persistent kernel).  Lines printed (rank 0, one JSON line):
   value      trajectories/s with inputs resident in HBM (device-timed, L2 flushed between steps)
-  e2e        the same through the C ABI with host buffers (degpu_batch_solve_host: H2D of
-             u0/p/tspan/saveat and D2H of ts/us/retcode inside the timed region)
+  e2e        the same through the C ABI with page-locked host buffers (degpu_batch_solve_host:
+             H2D of u0/p/tspan/saveat, and ts/us/retcode written by the solver kernel into
+             the host buffers over NVLink-C2C, inside the timed region)
   roofline   FP32 FLOP/s of the stepping kernel (algorithmic flops from the per-trajectory
              accept/reject counters) against a live FP32-FMA peak measurement
   cpu_baseline  the oracle's C++ restatement of the reference's kernel path on the host cores
@@ -447,6 +448,8 @@ def gpu_arm(args):
         same = np.array_equal(hus.numpy().view(np.uint32), us_h.view(np.uint32))
         e2e = {"value": B / e2e_s, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3, "api": "degpu_batch_solve_host",
+               "transfer": "inputs copied to HBM; outputs written by the solver kernel into the page-locked "
+                           "host buffers over NVLink-C2C",
                "controller": "plain", "matches_device_run": bool(same)}
 
     if rank != 0:

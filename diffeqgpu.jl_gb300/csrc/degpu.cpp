@@ -273,6 +273,46 @@ int ensure_context() {
   return 0;
 }
 
+// Device scratch of the library (persistent-driver work counters, the learned solve's
+// scratch, the host API's staging arena) comes from one memory pool per device that keeps
+// its memory between calls (release threshold unlimited; degpu_trim_memory returns it), so
+// repeated solves do not map and unmap device memory at every synchronisation as the
+// default pool (threshold 0) does.  Inside a stream capture the allocation goes to the
+// stream-ordered allocator's default pool instead (a graph allocation node).
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[64] = {};
+int lib_alloc(void** p, size_t n, cudaStream_t s) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    CUDA_TRY(cudaMallocAsync(p, n, s));
+    return 0;
+  }
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  cudaMemPool_t pool = nullptr;
+  if (dev >= 0 && dev < 64) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pools[dev]) {
+      cudaMemPoolProps props;
+      memset(&props, 0, sizeof props);
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      cudaMemPool_t np = nullptr;
+      if (cudaMemPoolCreate(&np, &props) == cudaSuccess) {
+        unsigned long long keep = ~0ULL;
+        cudaMemPoolSetAttribute(np, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pools[dev] = np;
+      }
+    }
+    pool = g_pools[dev];
+  }
+  if (pool) CUDA_TRY(cudaMallocFromPoolAsync(p, n, pool, s));
+  else CUDA_TRY(cudaMallocAsync(p, n, s));
+  return 0;
+}
+
 int get_kernel(const degpu_rhs_s* f, const KernelSpec& k, Kernel* out) {
   int rc = ensure_context();
   if (rc) return rc;
@@ -500,7 +540,10 @@ int run(const degpu_rhs* f, const degpu_problems* pr, const degpu_options* o, in
   }
   unsigned long long* work = nullptr;
   cudaStream_t s = (cudaStream_t)stream;
-  if (rq.spec.driver == 2) CUDA_TRY(cudaMallocAsync((void**)&work, 256, s));
+  if (rq.spec.driver == 2) {
+    rc = lib_alloc((void**)&work, 256, s);
+    if (rc) return rc;
+  }
   rc = launch(rq, K, block, chunk, work, (CUstream)s);
   if (work) cudaFreeAsync(work, s);
   return rc;
@@ -512,6 +555,11 @@ int run(const degpu_rhs* f, const degpu_problems* pr, const degpu_options* o, in
 extern "C" {
 
 const char* degpu_version(void) { return DEGPU_VERSION; }
+void degpu_trim_memory(void) {
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  for (int d = 0; d < 64; d++)
+    if (g_pools[d]) cudaMemPoolTrimTo(g_pools[d], 0);
+}
 void degpu_abi_struct_sizes(int* options, int* outputs, int* problems, int* continuous_callback, int* callbacks) {
   if (options) *options = (int)sizeof(degpu_options);
   if (outputs) *outputs = (int)sizeof(degpu_outputs);
@@ -575,46 +623,169 @@ int degpu_batch_solve_host(const degpu_rhs* f, const float* u0, const float* p, 
   if (B == 0) return 0;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t tsz = opt->time_type == DEGPU_TIME_F64 ? 8 : 4;
-  const size_t n_u0 = (size_t)B * f->N * 4, n_p = (size_t)B * f->P * 4, n_tsp = (size_t)B * 2 * tsz;
-  const size_t n_ts = (size_t)B * L * tsz, n_us = (size_t)B * L * f->N * 4;
-  const size_t n_sa = opt->nsaveat ? (size_t)opt->nsaveat * (opt->saveat_per_traj ? B : 1) * tsz : 0;
+  const size_t N = f->N, P = f->P;
+  const size_t n_u0 = (size_t)B * N * 4, n_p = (size_t)B * P * 4, n_tsp = (size_t)B * 2 * tsz;
+  const size_t n_ts = (size_t)B * L * tsz, n_us = (size_t)B * L * N * 4;
+  const size_t sa_rows = opt->nsaveat ? (opt->saveat_per_traj ? (size_t)B : 1) : 0;
+  const size_t n_sa = sa_rows * (size_t)opt->nsaveat * tsz;
+
+  // Output buffers in page-locked host memory are addressable by the GPU (unified addressing
+  // maps them into its address space; on GB300 they sit across the coherent NVLink-C2C
+  // link), so the solver kernel writes ts/us/retcodes into them itself: no device staging of
+  // the outputs and no copy pass after the solve.  Pageable outputs take the staged,
+  // pipelined path below.
+  auto device_view = [](const void* h) -> void* {
+    if (!h) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
+  };
+  const char* direct_env = getenv("DEGPU_HOST_DIRECT");
+  if (!(direct_env && direct_env[0] == '0')) {
+    void* v_ts = device_view(ts);
+    void* v_us = device_view(us);
+    void* v_rc = device_view(retcode);
+    void* v_na = device_view(naccept);
+    void* v_nr = device_view(nreject);
+    if (v_ts && v_us && (!retcode || v_rc) && (!naccept || v_na) && (!nreject || v_nr)) {
+      size_t o_u0 = 0, o_p = (o_u0 + n_u0 + 255) & ~(size_t)255, o_tsp = (o_p + n_p + 255) & ~(size_t)255;
+      size_t o_sa = (o_tsp + n_tsp + 255) & ~(size_t)255, o_work = (o_sa + n_sa + 255) & ~(size_t)255;
+      char* d = nullptr;
+      int rc = lib_alloc((void**)&d, o_work + 256, s);
+      if (rc) return rc;
+      if (cudaMemcpyAsync(d + o_u0, u0, n_u0, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+          (n_p && cudaMemcpyAsync(d + o_p, p, n_p, cudaMemcpyHostToDevice, s) != cudaSuccess) ||
+          cudaMemcpyAsync(d + o_tsp, tspan, n_tsp, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+          (n_sa && cudaMemcpyAsync(d + o_sa, opt->saveat, n_sa, cudaMemcpyHostToDevice, s) != cudaSuccess))
+        rc = fail(DEGPU_E_CUDA, "host-to-device copy failed");
+      if (!rc) {
+        degpu_problems pr{(const float*)(d + o_u0), (const float*)(d + o_p), d + o_tsp, B};
+        degpu_options o = *opt;
+        if (n_sa) o.saveat = d + o_sa;
+        degpu_outputs out{v_ts, (float*)v_us, L, (signed char*)v_rc, (int*)v_na, (int*)v_nr, nullptr};
+        unsigned long long* work = reinterpret_cast<unsigned long long*>(d + o_work);
+        rc = (opt->alg == DEGPU_ALG_EM) ? degpu_vectorized_solve_sde(f, &pr, &o, &out, s)
+                                        : (adaptive ? degpu_internal_asolve_with_work(f, &pr, &o, &out, work, s)
+                                                    : degpu_vectorized_solve(f, &pr, &o, &out, s));
+      }
+      cudaFreeAsync(d, s);
+      cudaError_t e = cudaStreamSynchronize(s);
+      if (!rc && e != cudaSuccess) rc = fail(DEGPU_E_CUDA, std::string("solve failed: ") + cudaGetErrorString(e));
+      return rc;
+    }
+  }
+
   // one device arena for inputs + outputs, freed stream-ordered at the end
   size_t off_u0 = 0, off_p = (off_u0 + n_u0 + 255) & ~(size_t)255, off_tsp = (off_p + n_p + 255) & ~(size_t)255;
   size_t off_sa = (off_tsp + n_tsp + 255) & ~(size_t)255, off_ts = (off_sa + n_sa + 255) & ~(size_t)255;
   size_t off_us = (off_ts + n_ts + 255) & ~(size_t)255, off_rc = (off_us + n_us + 255) & ~(size_t)255;
   size_t off_na = (off_rc + B + 255) & ~(size_t)255, off_nr = (off_na + 4 * B + 255) & ~(size_t)255;
-  size_t total = off_nr + 4 * B;
+  long long chunk = B;
+  if (B >= 2 * 262144) chunk = std::max<long long>(262144, (B + 7) / 8);
+  if (const char* e = getenv("DEGPU_HOST_CHUNK")) {
+    long long v = atoll(e);
+    if (v > 0) chunk = v;
+  }
+  const long long nchunks = (B + chunk - 1) / chunk;
+  // one 256-byte persistent-driver work counter per chunk, so no chunk allocates on its own
+  size_t off_work = (off_nr + 4 * B + 255) & ~(size_t)255;
+  size_t total = off_work + 256 * (size_t)nchunks;
   char* d = nullptr;
-  CUDA_TRY(cudaMallocAsync((void**)&d, total, s));
+  {
+    int arc = lib_alloc((void**)&d, total, s);
+    if (arc) return arc;
+  }
+  // Pipelined: the batch is cut into chunks of contiguous trajectories.  The chunks' solves
+  // alternate between two compute streams (so one chunk's tail overlaps the next chunk's
+  // start), and a third stream copies each finished chunk back while later chunks solve (the
+  // copy engines and the SMs work at once).  Chunking changes no result: trajectories are
+  // independent and the noise streams are keyed by the global trajectory index
+  // (traj_offset).
+  const bool piped = nchunks > 1;
+  cudaStream_t comp[2] = {s, s}, out_s = s;
+  cudaEvent_t ev_start = nullptr, ev_k[2] = {nullptr, nullptr}, ev_end[3] = {nullptr, nullptr, nullptr};
   int rc = 0;
-  do {
-    if (cudaMemcpyAsync(d + off_u0, u0, n_u0, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        (n_p && cudaMemcpyAsync(d + off_p, p, n_p, cudaMemcpyHostToDevice, s) != cudaSuccess) ||
-        cudaMemcpyAsync(d + off_tsp, tspan, n_tsp, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        (n_sa && cudaMemcpyAsync(d + off_sa, opt->saveat, n_sa, cudaMemcpyHostToDevice, s) != cudaSuccess)) {
+  auto cleanup_streams = [&]() {
+    for (int k = 0; k < 2; k++) {
+      if (ev_k[k]) cudaEventDestroy(ev_k[k]);
+      if (comp[k] != s) cudaStreamDestroy(comp[k]);
+    }
+    for (int k = 0; k < 3; k++)
+      if (ev_end[k]) cudaEventDestroy(ev_end[k]);
+    if (out_s != s) cudaStreamDestroy(out_s);
+    if (ev_start) cudaEventDestroy(ev_start);
+  };
+  if (!rc && n_sa && !opt->saveat_per_traj &&
+      cudaMemcpyAsync(d + off_sa, opt->saveat, n_sa, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    rc = fail(DEGPU_E_CUDA, "host-to-device copy failed");
+  if (!rc && piped) {
+    bool ok = cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventRecord(ev_start, s) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&out_s, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamWaitEvent(out_s, ev_start, 0) == cudaSuccess;
+    for (int k = 0; k < 2 && ok; k++)
+      ok = cudaStreamCreateWithFlags(&comp[k], cudaStreamNonBlocking) == cudaSuccess &&
+           cudaEventCreateWithFlags(&ev_k[k], cudaEventDisableTiming) == cudaSuccess &&
+           cudaStreamWaitEvent(comp[k], ev_start, 0) == cudaSuccess;
+    for (int k = 0; k < 3 && ok; k++) ok = cudaEventCreateWithFlags(&ev_end[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) rc = fail(DEGPU_E_CUDA, "pipeline stream set-up failed");
+  }
+  for (long long c0 = 0, ci = 0; c0 < B && !rc; c0 += chunk, ci++) {
+    const long long nb = std::min(chunk, B - c0);
+    cudaStream_t cs = comp[ci & 1];
+    auto h2d = [&](size_t off, const void* src, size_t unit) {
+      return unit == 0 || cudaMemcpyAsync(d + off + c0 * unit, (const char*)src + c0 * unit, nb * unit,
+                                          cudaMemcpyHostToDevice, cs) == cudaSuccess;
+    };
+    auto d2h = [&](void* dst, size_t off, size_t unit) {
+      return !dst || cudaMemcpyAsync((char*)dst + c0 * unit, d + off + c0 * unit, nb * unit, cudaMemcpyDeviceToHost,
+                                     out_s) == cudaSuccess;
+    };
+    const size_t sa_unit = opt->saveat_per_traj ? (size_t)opt->nsaveat * tsz : 0;
+    if (!h2d(off_u0, u0, N * 4) || !(P == 0 || h2d(off_p, p, P * 4)) || !h2d(off_tsp, tspan, 2 * tsz) ||
+        !(sa_unit == 0 || h2d(off_sa, opt->saveat, sa_unit))) {
       rc = fail(DEGPU_E_CUDA, "host-to-device copy failed");
       break;
     }
-    degpu_problems pr{(const float*)(d + off_u0), (const float*)(d + off_p), d + off_tsp, B};
+    degpu_problems pr{(const float*)(d + off_u0) + c0 * N, (const float*)(d + off_p) + c0 * P,
+                      d + off_tsp + c0 * 2 * tsz, nb};
     degpu_options o = *opt;
-    if (n_sa) o.saveat = d + off_sa;
-    degpu_outputs out{d + off_ts, (float*)(d + off_us), L, retcode ? (signed char*)(d + off_rc) : nullptr,
-                      naccept ? (int*)(d + off_na) : nullptr, nreject ? (int*)(d + off_nr) : nullptr, nullptr};
-    rc = (opt->alg == DEGPU_ALG_EM) ? degpu_vectorized_solve_sde(f, &pr, &o, &out, s)
-                                    : (adaptive ? degpu_vectorized_asolve(f, &pr, &o, &out, s)
-                                                : degpu_vectorized_solve(f, &pr, &o, &out, s));
+    o.traj_offset = opt->traj_offset + c0;
+    if (n_sa) o.saveat = d + off_sa + c0 * sa_unit;
+    if (o.dt0) o.dt0 = opt->dt0 + c0;  // per-trajectory device arrays of the whole batch
+    if (o.tolscale) o.tolscale = opt->tolscale + c0;
+    degpu_outputs out{d + off_ts + c0 * L * tsz, (float*)(d + off_us) + c0 * L * N, L,
+                      retcode ? (signed char*)(d + off_rc) + c0 : nullptr, naccept ? (int*)(d + off_na) + c0 : nullptr,
+                      nreject ? (int*)(d + off_nr) + c0 : nullptr, nullptr};
+    unsigned long long* work = reinterpret_cast<unsigned long long*>(d + off_work + 256 * (size_t)ci);
+    rc = (opt->alg == DEGPU_ALG_EM) ? degpu_vectorized_solve_sde(f, &pr, &o, &out, cs)
+                                    : (adaptive ? degpu_internal_asolve_with_work(f, &pr, &o, &out, work, cs)
+                                                : degpu_vectorized_solve(f, &pr, &o, &out, cs));
     if (rc) break;
-    if (cudaMemcpyAsync(ts, d + off_ts, n_ts, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(us, d + off_us, n_us, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        (retcode && cudaMemcpyAsync(retcode, d + off_rc, B, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
-        (naccept && cudaMemcpyAsync(naccept, d + off_na, 4 * B, cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
-        (nreject && cudaMemcpyAsync(nreject, d + off_nr, 4 * B, cudaMemcpyDeviceToHost, s) != cudaSuccess)) {
+    if (piped && (cudaEventRecord(ev_k[ci & 1], cs) != cudaSuccess ||
+                  cudaStreamWaitEvent(out_s, ev_k[ci & 1], 0) != cudaSuccess)) {
+      rc = fail(DEGPU_E_CUDA, "pipeline event failed");
+      break;
+    }
+    if (!d2h(ts, off_ts, L * tsz) || !d2h(us, off_us, L * N * 4) || !d2h(retcode, off_rc, 1) ||
+        !d2h(naccept, off_na, 4) || !d2h(nreject, off_nr, 4)) {
       rc = fail(DEGPU_E_CUDA, "device-to-host copy failed");
       break;
     }
-  } while (0);
+  }
+  if (piped && ev_end[2]) {  // join every pipeline stream back into the caller's stream
+    cudaStream_t js[3] = {comp[0], comp[1], out_s};
+    for (int k = 0; k < 3; k++) {
+      cudaEventRecord(ev_end[k], js[k]);
+      cudaStreamWaitEvent(s, ev_end[k], 0);
+    }
+  }
   cudaFreeAsync(d, s);
   cudaError_t e = cudaStreamSynchronize(s);
+  cleanup_streams();
   if (!rc && e != cudaSuccess) rc = fail(DEGPU_E_CUDA, std::string("solve failed: ") + cudaGetErrorString(e));
   return rc;
 }
@@ -663,8 +834,9 @@ int degpu_learned_asolve(const degpu_rhs* f, const degpu_mlp* m, const degpu_pro
   if (!(s_max >= 1.0f) || !(dt_lo > 0.0f) || !(dt_hi >= dt_lo)) return fail(DEGPU_E_INVALID, "bad dt / scale clamp");
   cudaStream_t s = (cudaStream_t)stream;
   float* scratch = nullptr;  // dt0 [B] followed by tolscale [B]
-  CUDA_TRY(cudaMallocAsync((void**)&scratch, sizeof(float) * 2 * (size_t)probs->B, s));
-  int rc = degpu_mlp_infer_problems(m, probs->u0, f->N, probs->p, f->P, (float)opt->reltol, probs->B, scratch,
+  int rc = lib_alloc((void**)&scratch, sizeof(float) * 2 * (size_t)probs->B, s);
+  if (rc) return rc;
+  rc = degpu_mlp_infer_problems(m, probs->u0, f->N, probs->p, f->P, (float)opt->reltol, probs->B, scratch,
                                     scratch + probs->B, dt_lo, dt_hi, 1.0f, s_max, stream);
   if (rc) rc = fail(rc, "step-size model inference failed (does the model's input width match N + P + 1?)");
   if (!rc) {
@@ -694,7 +866,8 @@ int degpu_autotune(const degpu_rhs* f, const degpu_problems* probs, const degpu_
   std::vector<int> chunks = {0};
   if (rq.spec.driver == 2) chunks = {32, 64, 128};
   unsigned long long* work = nullptr;
-  CUDA_TRY(cudaMallocAsync((void**)&work, 256, s));
+  rc = lib_alloc((void**)&work, 256, s);
+  if (rc) return rc;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

@@ -919,25 +919,30 @@ DEGPU_DEV void run_affect(Lane& L, int kind, int fn) {
 #endif
 
 #if DEGPU_NCCB > 0
-// Julia's sign / eps / nextfloat / max on the time type (ITP root finder)
+// Event times.  Float32 tspan: absolute times in Float32, every operation the reference's.
+// FP64 tspan: float offsets from tprev -- the located time is tprev + x in the float-pair
+// time, and root finding runs on the FP32 pipes (the FP32 interpolant it brackets resolves
+// no finer than a float offset within one step; GB300 runs FP64 at 1/64 of the FP32 rate).
+#if DEGPU_TIME_DF
+DEGPU_DEV float cb_bottom(const Lane& L) { return 0.0f; }
+DEGPU_DEV float cb_top(const Lane& L) { return TP::rem(L.t, L.tprev, 0.0f); }
+DEGPU_DEV float cb_theta(const Lane& L, float x) { return x / L.dt; }
+DEGPU_DEV Time cb_time(const Lane& L, float x) { return TP::add(L.tprev, x); }
+#else
+DEGPU_DEV float cb_bottom(const Lane& L) { return L.tprev; }
+DEGPU_DEV float cb_top(const Lane& L) { return L.t; }
+DEGPU_DEV float cb_theta(const Lane& L, float x) { return (x - L.tprev) / L.dt; }
+DEGPU_DEV Time cb_time(const Lane& L, float x) { return x; }
+#endif
+
+// Julia's sign / eps / nextfloat / max on Float32 (ITP root finder)
 DEGPU_DEV float jl_sign(float x) { return (x == 0.0f || x != x) ? x : copysignf(1.0f, x); }
-DEGPU_DEV float t_abs(float x) { return fabsf(x); }
-DEGPU_DEV double t_abs(double x) { return fabs(x); }
-DEGPU_DEV float t_copysign(float a, float b) { return copysignf(a, b); }
-DEGPU_DEV double t_copysign(double a, double b) { return copysign(a, b); }
 DEGPU_DEV float t_max(float x, float y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
-DEGPU_DEV double t_max(double x, double y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
-DEGPU_DEV float t_eps(float x) {  // ldexp(eps(T), exponent(x)); nextfloat(0) below floatmin
+DEGPU_DEV float t_eps(float x) {  // ldexp(eps(Float32), exponent(x)); nextfloat(0) below floatmin
   const unsigned e = (__float_as_uint(x) >> 23) & 0xffu;
   if (e == 0xffu) return __uint_as_float(0x7fc00000u);
   if (e > 23u) return __uint_as_float((e - 23u) << 23);
   return __uint_as_float(e == 0u ? 1u : (1u << (e - 1u)));
-}
-DEGPU_DEV double t_eps(double x) {
-  const unsigned long long e = ((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffull;
-  if (e == 0x7ffull) return __longlong_as_double(0x7ff8000000000000ll);
-  if (e > 52ull) return __longlong_as_double((long long)((e - 52ull) << 52));
-  return __longlong_as_double((long long)(e == 0ull ? 1ull : (1ull << (e - 1ull))));
 }
 DEGPU_DEV float t_nextfloat(float x) {
   if (x != x || x == __int_as_float(0x7f800000)) return x;
@@ -945,76 +950,69 @@ DEGPU_DEV float t_nextfloat(float x) {
   const unsigned b = __float_as_uint(x);
   return __uint_as_float(x > 0.0f ? b + 1u : b - 1u);
 }
-DEGPU_DEV double t_nextfloat(double x) {
-  if (x != x || x == __longlong_as_double(0x7ff0000000000000ll)) return x;
-  if (x == 0.0) return __longlong_as_double(1ll);
-  const long long b = __double_as_longlong(x);
-  return __longlong_as_double(x > 0.0 ? b + 1 : b - 1);
-}
 
 // get_condition (integrator_utils.jl:461-479): u at t, uprev at tprev, else integ(abst)
-DEGPU_DEV float ccb_condition_at(const Lane& L, int fn, Tt abst) {
-  float x[N];
-  if (abst == (Tt)TP::out(L.t)) {
+DEGPU_DEV float ccb_condition_at(const Lane& L, int fn, float x) {
+  float v[N];
+  if (x == cb_top(L)) {
 #pragma unroll
-    for (int c = 0; c < N; c++) x[c] = L.u[c];
-  } else if (abst == (Tt)TP::out(L.tprev)) {
+    for (int c = 0; c < N; c++) v[c] = L.u[c];
+  } else if (x == cb_bottom(L)) {
 #pragma unroll
-    for (int c = 0; c < N; c++) x[c] = L.uprev[c];
+    for (int c = 0; c < N; c++) v[c] = L.uprev[c];
   } else {
-    interp(L, TP::theta(TP::from(abst), L.tprev, L.dt), L.dt, x);
+    interp(L, cb_theta(L, x), L.dt, v);
   }
-  return (float)degpu_ccb_condition(fn, x, L.p, abst);
+  return (float)degpu_ccb_condition(fn, v, L.p, (Tt)TP::out(cb_time(L, x)));
 }
 
 // gpu_find_root (integrator_utils.jl:302-355): ITP with scaled_k1 = 0.2, k2 = 2, n0 = 10,
-// at most 100 iterations, in the time type
-DEGPU_DEV Tt itp_root(const Lane& L, int fn, Tt left, Tt right, int rootfind) {
+// at most 100 iterations
+DEGPU_DEV float itp_root(const Lane& L, int fn, float left, float right, int rootfind) {
   float fl = ccb_condition_at(L, fn, left);
   float fr = ccb_condition_at(L, fn, right);
-  const Tt span0 = right - left;
-  const Tt k1 = (Tt)0.2 / span0;
-  Tt eps_s = span0 * (Tt)512;
+  const float span0 = right - left;
+  const float k1 = 0.2f / span0;
+  float eps_s = span0 * 512.0f;
   for (int it = 0; it < 100; it++) {
-    const Tt span = right - left;
-    const Tt mid = (left + right) / (Tt)2;
-    const Tt r = eps_s - span / (Tt)2;
-    const Tt x_f = left + (span * (Tt)fl) / (Tt)(fl - fr);
-    const Tt delta = t_max(k1 * span * span, t_eps(x_f));
-    const Tt diff = mid - x_f;
-    const Tt xt = (delta <= t_abs(diff)) ? x_f + t_copysign(delta, diff) : mid;
-    const Tt xp = (t_abs(xt - mid) <= r) ? xt : mid - t_copysign(r, diff);
+    const float span = right - left;
+    const float mid = (left + right) / 2.0f;
+    const float r = eps_s - span / 2.0f;
+    const float x_f = left + (span * fl) / (fl - fr);
+    const float delta = t_max(k1 * span * span, t_eps(x_f));
+    const float diff = mid - x_f;
+    const float xt = (delta <= fabsf(diff)) ? x_f + copysignf(delta, diff) : mid;
+    const float xp = (fabsf(xt - mid) <= r) ? xt : mid - copysignf(r, diff);
     const float yp = ccb_condition_at(L, fn, xp);
     const float yps = yp * jl_sign(fr);
     if (yps > 0.0f) { right = xp; fr = yp; }
     else if (yps < 0.0f) { left = xp; fl = yp; }
     else { left = xp; right = xp; break; }
-    eps_s = eps_s / (Tt)2;
+    eps_s = eps_s / 2.0f;
     if (t_nextfloat(left) >= right) break;
   }
   return rootfind == 1 ? right : left;  // SciMLBase.RightRootFind : LeftRootFind
 }
 
 struct CbEvent {
-  Tt t;
-  float prev_sign, residual;
+  float t, prev_sign, residual;
   bool occurred;
 };
 // find_callback_time (integrator_utils.jl:357-428) for member j of the set
 DEGPU_DEV CbEvent find_callback_time(const Lane& L, const Io& io, int j) {
   const int fn = io.P.ccb_fn[j], fl = io.P.ccb_flags[j];
-  float x[N];
+  float v[N];
 #pragma unroll
-  for (int c = 0; c < N; c++) x[c] = L.uprev[c];
-  Tt bottom_t = (Tt)TP::out(L.tprev);
-  float bottom_c = (float)degpu_ccb_condition(fn, x, L.p, bottom_t);
+  for (int c = 0; c < N; c++) v[c] = L.uprev[c];
+  float bottom_t = cb_bottom(L);
+  float bottom_c = (float)degpu_ccb_condition(fn, v, L.p, (Tt)TP::out(L.tprev));
   if (L.event_last == j + 1 && fabsf(bottom_c - L.last_event_error) <= io.P.ccb_abstol[j]) {
     // nudge past the previous event's root so that it is not found again
-    bottom_t = bottom_t + (Tt)(L.dt * io.P.ccb_nudge[j]);
+    bottom_t = bottom_t + L.dt * io.P.ccb_nudge[j];
     bottom_c = ccb_condition_at(L, fn, bottom_t);
   }
   const float bs = jl_sign(bottom_c);
-  const Tt top_t = (Tt)TP::out(L.t);
+  const float top_t = cb_top(L);
   const float ts_ = jl_sign(ccb_condition_at(L, fn, top_t));
   CbEvent e;
   e.prev_sign = bs;
@@ -1030,15 +1028,15 @@ DEGPU_DEV CbEvent find_callback_time(const Lane& L, const Io& io, int j) {
 }
 
 // change_t_via_interpolation! (integrator_utils.jl:180-209)
-DEGPU_DEV void change_t_via_interpolation(Lane& L, Tt tnew) {
-  const Tt tcur = (Tt)TP::out(L.t);
-  if (tnew != tcur) {
+DEGPU_DEV void change_t_via_interpolation(Lane& L, float x) {
+  const float xcur = cb_top(L);
+  if (x != xcur) {
     float v[N];
-    interp(L, TP::theta(TP::from(tnew), L.tprev, L.dt), L.dt, v);
+    interp(L, cb_theta(L, x), L.dt, v);
 #pragma unroll
     for (int c = 0; c < N; c++) L.u[c] = v[c];
-    L.step_idx -= (int)rint((tcur - tnew) / (Tt)L.dt);
-    L.t = TP::from(tnew);
+    L.step_idx -= (int)rintf((xcur - x) / L.dt);
+    L.t = cb_time(L, x);
   }
 }
 #endif
@@ -1054,7 +1052,7 @@ DEGPU_DEV bool handle_callbacks(Lane& L, const Io& io, int i, bool save_every, b
 #if DEGPU_NCCB > 0
   CbEvent best;
   best.occurred = false;
-  best.t = (Tt)0;
+  best.t = 0.0f;
   best.prev_sign = 0.0f;
   best.residual = 0.0f;
   int idx = 0;
@@ -1067,10 +1065,10 @@ DEGPU_DEV bool handle_callbacks(Lane& L, const Io& io, int i, bool save_every, b
     L.event_last = idx;
     L.last_event_error = best.residual;
     change_t_via_interpolation(L, best.t);
-    if (ADAPTIVE && L.dtnew < 1.0e-12f) {
-      const Tt remaining = t_abs((Tt)TP::out(L.tf) - (Tt)TP::out(L.t));
-      const Tt relaxed = (Tt)(io.P.ccb_dtrelax[0] * L.dt);
-      L.dtnew = (float)((remaining < relaxed) ? remaining : relaxed);
+    if (ADAPTIVE && L.dtnew < 1.0e-12f) {  // :226-234
+      const float remaining = fabsf(TP::rem(L.tf, L.t, 0.0f));
+      const float relaxed = io.P.ccb_dtrelax[0] * L.dt;
+      L.dtnew = (remaining < relaxed) ? remaining : relaxed;
     }
     save_values(L, io, i, save_every);
     saved = true;

@@ -67,6 +67,7 @@ class DegpuError(RuntimeError):
 _P = ctypes.c_void_p
 SIGNATURES = {
     "degpu_version": (ctypes.c_char_p, []),
+    "degpu_trim_memory": (None, []),
     "degpu_abi_struct_sizes": (None, [ctypes.POINTER(ctypes.c_int)] * 5),
     "degpu_last_error": (ctypes.c_char_p, []),
     "degpu_rhs_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),

@@ -148,6 +148,9 @@ const char* degpu_version(void);
 /* sizeof of the ABI structs (options, outputs, problems, continuous callback, callback set),
  * so that bindings can check their mirrors of these layouts */
 void degpu_abi_struct_sizes(int* options, int* outputs, int* problems, int* continuous_callback, int* callbacks);
+/* The library keeps the device scratch of earlier solves (work counters, the host API's
+ * staging arena) in a per-device memory pool for reuse; this returns it to the device. */
+void degpu_trim_memory(void);
 /* last error message of the calling thread */
 const char* degpu_last_error(void);
 
@@ -182,7 +185,13 @@ int degpu_vectorized_solve_sde(const degpu_rhs* f, const degpu_problems* probs, 
 
 /* batch_solve_up_kernel (src/solve.jl:382-419) with HOST buffers: copies the problems
  * to the device, runs vectorized_(a)solve, copies ts/us (and retcodes) back and
- * synchronises.  adaptive selects vectorized_asolve.  Host arrays use the layouts above. */
+ * synchronises.  adaptive selects vectorized_asolve.  Host arrays use the layouts above
+ * opt->saveat is a host array here, opt->dt0 / opt->tolscale stay device arrays.  Outputs
+ * in page-locked memory (cudaHostAlloc / cudaHostRegister) are written by the solver kernel
+ * directly (environment DEGPU_HOST_DIRECT=0 turns that off); pageable outputs are staged on
+ * the device and, from 524,288 trajectories, pipelined in chunks (two compute streams and one
+ * copy-back stream; environment DEGPU_HOST_CHUNK sets the chunk size).  Results do not depend
+ * on the path or the chunking. */
 int degpu_batch_solve_host(const degpu_rhs* f, const float* u0, const float* p, const void* tspan, long long B,
                            const degpu_options* opt, int adaptive, void* ts, float* us, int L,
                            signed char* retcode, int* naccept, int* nreject, void* stream);

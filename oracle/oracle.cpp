@@ -712,14 +712,12 @@ static void interpolate(int m, int alg, const Integ<Tt>& ig, const float* p, flo
 }
 
 /* ------------------------------------------------------------------ callbacks (integrator_utils.jl:52-479)
- * Julia's sign / eps / nextfloat / max on the time type, the ITP root finder, event location
- * and application.  To is the time type at the boundary (float, or double for the pair time). */
+ * Julia's sign / eps / nextfloat / max on Float32, the ITP root finder, event location and
+ * application.  Event times: with a Float32 tspan absolute Float32 times (the reference's
+ * arithmetic); with an FP64 tspan float offsets x from tprev, the event at tprev + x in the
+ * pair time (the kernels do the same: the FP32 interpolant resolves no finer). */
 static inline float jl_sign(float x) { return (x == 0.0f || x != x) ? x : copysignf(1.0f, x); }
-static inline float o_abs(float x) { return fabsf(x); }
-static inline double o_abs(double x) { return fabs(x); }
-static inline float o_copysign(float a, float b) { return copysignf(a, b); }
-static inline double o_copysign(double a, double b) { return copysign(a, b); }
-template <class To> static inline To o_max(To x, To y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
+static inline float o_max(float x, float y) { if (x != x) return x; if (y != y) return y; return y > x ? y : x; }
 static inline float o_eps(float x) { /* ldexp(eps(Float32), exponent(x)); nextfloat(0) below floatmin */
   uint32_t b; memcpy(&b, &x, 4);
   uint32_t e = (b >> 23) & 0xffu, r;
@@ -728,62 +726,61 @@ static inline float o_eps(float x) { /* ldexp(eps(Float32), exponent(x)); nextfl
   else r = e == 0u ? 1u : (1u << (e - 1u));
   float y; memcpy(&y, &r, 4); return y;
 }
-static inline double o_eps(double x) {
-  uint64_t b; memcpy(&b, &x, 8);
-  uint64_t e = (b >> 52) & 0x7ffull, r;
-  if (e == 0x7ffull) r = 0x7ff8000000000000ull;
-  else if (e > 52ull) r = (e - 52ull) << 52;
-  else r = e == 0ull ? 1ull : (1ull << (e - 1ull));
-  double y; memcpy(&y, &r, 8); return y;
-}
 static inline float o_nextfloat(float x) {
   if (x != x || x == INFINITY) return x;
   uint32_t b;
   if (x == 0.0f) b = 1u; else { memcpy(&b, &x, 4); b = x > 0.0f ? b + 1u : b - 1u; }
   float y; memcpy(&y, &b, 4); return y;
 }
-static inline double o_nextfloat(double x) {
-  if (x != x || x == (double)INFINITY) return x;
-  uint64_t b;
-  if (x == 0.0) b = 1ull; else { memcpy(&b, &x, 8); b = x > 0.0 ? b + 1ull : b - 1ull; }
-  double y; memcpy(&y, &b, 8); return y;
-}
+
+template <class Tt> struct CbClock;
+template <> struct CbClock<float> {
+  static float bottom(const Integ<float>& ig) { return ig.tprev; }
+  static float top(const Integ<float>& ig) { return ig.t; }
+  static float theta(const Integ<float>& ig, float x) { return (x - ig.tprev) / ig.dt; }
+  static float time(const Integ<float>& ig, float x) { (void)ig; return x; }
+};
+template <> struct CbClock<DF> {
+  static float bottom(const Integ<DF>& ig) { (void)ig; return 0.0f; }
+  static float top(const Integ<DF>& ig) { return t_rem(ig.t, ig.tprev, 0.0f); }
+  static float theta(const Integ<DF>& ig, float x) { return x / ig.dt; }
+  static DF time(const Integ<DF>& ig, float x) { return t_add(ig.tprev, x); }
+};
 
 /* get_condition (integrator_utils.jl:461-479): u at t, uprev at tprev, else integ(abst) */
 template <class Tt>
-static float cond_at(int m, int alg, const Integ<Tt>& ig, const float* p, int fn, typename TOut<Tt>::T abst) {
-  typedef typename TOut<Tt>::T To;
-  float x[MAXN];
-  if (abst == (To)t_out(ig.t)) for (int c = 0; c < ig.N; c++) x[c] = ig.u[c];
-  else if (abst == (To)t_out(ig.tprev)) for (int c = 0; c < ig.N; c++) x[c] = ig.uprev[c];
-  else interpolate(m, alg, ig, p, t_theta(t_from<Tt>((double)abst), ig.tprev, ig.dt), ig.dt, x);
-  return model_ccb_condition(m, fn, x, p, (double)abst);
+static float cond_at(int m, int alg, const Integ<Tt>& ig, const float* p, int fn, float x) {
+  typedef CbClock<Tt> K;
+  float v[MAXN];
+  if (x == K::top(ig)) for (int c = 0; c < ig.N; c++) v[c] = ig.u[c];
+  else if (x == K::bottom(ig)) for (int c = 0; c < ig.N; c++) v[c] = ig.uprev[c];
+  else interpolate(m, alg, ig, p, K::theta(ig, x), ig.dt, v);
+  return model_ccb_condition(m, fn, v, p, (double)t_out(K::time(ig, x)));
 }
 
 /* gpu_find_root (integrator_utils.jl:302-355): ITP, scaled_k1 = 0.2, k2 = 2, n0 = 10 */
 template <class Tt>
-static typename TOut<Tt>::T itp_root(int m, int alg, const Integ<Tt>& ig, const float* p, int fn,
-                                     typename TOut<Tt>::T left, typename TOut<Tt>::T right, int rootfind) {
-  typedef typename TOut<Tt>::T To;
+static float itp_root(int m, int alg, const Integ<Tt>& ig, const float* p, int fn, float left, float right,
+                      int rootfind) {
   float fl = cond_at(m, alg, ig, p, fn, left), fr = cond_at(m, alg, ig, p, fn, right);
-  const To span0 = right - left;
-  const To k1 = (To)0.2 / span0;
-  To eps_s = span0 * (To)512;
+  const float span0 = right - left;
+  const float k1 = 0.2f / span0;
+  float eps_s = span0 * 512.0f;
   for (int it = 0; it < 100; it++) {
-    const To span = right - left;
-    const To mid = (left + right) / (To)2;
-    const To r = eps_s - span / (To)2;
-    const To x_f = left + (span * (To)fl) / (To)(fl - fr);
-    const To delta = o_max<To>(k1 * span * span, o_eps(x_f));
-    const To diff = mid - x_f;
-    const To xt = (delta <= o_abs(diff)) ? x_f + o_copysign(delta, diff) : mid;
-    const To xp = (o_abs(xt - mid) <= r) ? xt : mid - o_copysign(r, diff);
+    const float span = right - left;
+    const float mid = (left + right) / 2.0f;
+    const float r = eps_s - span / 2.0f;
+    const float x_f = left + (span * fl) / (fl - fr);
+    const float delta = o_max(k1 * span * span, o_eps(x_f));
+    const float diff = mid - x_f;
+    const float xt = (delta <= fabsf(diff)) ? x_f + copysignf(delta, diff) : mid;
+    const float xp = (fabsf(xt - mid) <= r) ? xt : mid - copysignf(r, diff);
     const float yp = cond_at(m, alg, ig, p, fn, xp);
     const float yps = yp * jl_sign(fr);
     if (yps > 0.0f) { right = xp; fr = yp; }
     else if (yps < 0.0f) { left = xp; fl = yp; }
     else { left = xp; right = xp; break; }
-    eps_s = eps_s / (To)2;
+    eps_s = eps_s / 2.0f;
     if (o_nextfloat(left) >= right) break;
   }
   return rootfind == 1 ? right : left;
@@ -827,27 +824,25 @@ static void run_affect(int m, Integ<Tt>& ig, const float* p, int kind, int fn) {
 template <class Tt>
 static int handle_callbacks(int m, const oracle_cfg* cfg, Integ<Tt>& ig, const float* p, const double* sa,
                             int nsa, int L, int save_every, typename TOut<Tt>::T* ts, float* us) {
-  typedef typename TOut<Tt>::T To;
+  typedef CbClock<Tt> K;
   const int alg = cfg->alg, N = ig.N;
   int saved = 0;
   if (cfg->nccb > 0) {
     int occ_best = 0, idx = 0;
-    To t_best = 0;
-    float sign_best = 0.0f, res_best = 0.0f;
+    float t_best = 0.0f, sign_best = 0.0f, res_best = 0.0f;
     for (int j = 0; j < cfg->nccb; j++) {
       const int fn = cfg->ccb_fn[j], fl = cfg->ccb_flags[j];
-      To bottom_t = (To)t_out(ig.tprev);
-      float bottom_c = model_ccb_condition(m, fn, ig.uprev, p, (double)bottom_t);
+      float bottom_t = K::bottom(ig);
+      float bottom_c = model_ccb_condition(m, fn, ig.uprev, p, (double)t_out(ig.tprev));
       if (ig.event_last == j + 1 && fabsf(bottom_c - ig.last_event_error) <= cfg->ccb_abstol[j]) {
-        bottom_t = bottom_t + (To)(ig.dt * cfg->ccb_nudge[j]);
+        bottom_t = bottom_t + ig.dt * cfg->ccb_nudge[j];
         bottom_c = cond_at(m, alg, ig, p, fn, bottom_t);
       }
       const float bs = jl_sign(bottom_c);
-      const To top_t = (To)t_out(ig.t);
+      const float top_t = K::top(ig);
       const float tsg = jl_sign(cond_at(m, alg, ig, p, fn, top_t));
       const int occ = ((bs < 0.0f && (fl & 1)) || (bs > 0.0f && (fl & 2))) && bs * tsg <= 0.0f;
-      To te = top_t;
-      float res = 0.0f;
+      float te = top_t, res = 0.0f;
       const int rootfind = (fl >> 2) & 3;
       if (occ && rootfind != 2 && tsg != 0.0f) {
         te = itp_root(m, alg, ig, p, fn, bottom_t, top_t, rootfind);
@@ -858,19 +853,18 @@ static int handle_callbacks(int m, const oracle_cfg* cfg, Integ<Tt>& ig, const f
     if (occ_best) {
       ig.event_last = idx;
       ig.last_event_error = res_best;
-      const To tcur = (To)t_out(ig.t);
-      if (t_best != tcur) {
+      const float xcur = K::top(ig);
+      if (t_best != xcur) { /* change_t_via_interpolation! (:180-209) */
         float v[MAXN];
-        interpolate(m, alg, ig, p, t_theta(t_from<Tt>((double)t_best), ig.tprev, ig.dt), ig.dt, v);
+        interpolate(m, alg, ig, p, K::theta(ig, t_best), ig.dt, v);
         for (int c = 0; c < N; c++) ig.u[c] = v[c];
-        To q = (tcur - t_best) / (To)ig.dt;
-        ig.step_idx -= (int)(sizeof(To) == 8 ? rint((double)q) : rintf((float)q));
-        ig.t = t_from<Tt>((double)t_best);
+        ig.step_idx -= (int)rintf((xcur - t_best) / ig.dt);
+        ig.t = K::time(ig, t_best);
       }
-      if (cfg->adaptive && ig.dtnew < 1.0e-12f) {
-        const To remaining = o_abs((To)t_out(ig.tf) - (To)t_out(ig.t));
-        const To relaxed = (To)(cfg->ccb_dtrelax[0] * ig.dt);
-        ig.dtnew = (float)((remaining < relaxed) ? remaining : relaxed);
+      if (cfg->adaptive && ig.dtnew < 1.0e-12f) { /* :226-234 */
+        const float remaining = fabsf(t_rem(ig.tf, ig.t, 0.0f));
+        const float relaxed = cfg->ccb_dtrelax[0] * ig.dt;
+        ig.dtnew = (remaining < relaxed) ? remaining : relaxed;
       }
       save_values(m, alg, ig, p, sa, nsa, L, save_every, ts, us);
       saved = 1;
