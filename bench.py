@@ -105,45 +105,70 @@ def reference_arm(args):
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-             "clocks_event_reasons.sw_power_cap")
+    """nvidia-smi clock / throttle-reason samples every 20 ms, started before the timed region
+    (the context waits for the first sample) and filtered to the region's wall-clock span."""
+    QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index=0):
         self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
         self.proc = None
         self.gpu = gpu_index
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.path.parent.mkdir(exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
+            deadline = time.time() + 10
+            while time.time() < deadline and self.path.stat().st_size == 0 and self.proc.poll() is None:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
         return self
 
+    def mark(self, start: bool):
+        if start:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
+
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(0.05)
             self.proc.terminate()
             self.proc.wait()
             self.f.close()
 
     def summary(self):
+        import datetime
         try:
             rows = [r.split(", ") for r in self.path.read_text().strip().splitlines() if r.strip()]
         except Exception:
             return None
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+
+        def stamp(r):
+            try:
+                return datetime.datetime.strptime(r[0].strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except Exception:
+                return None
+        inside = [r for r in rows if self.t0 and self.t1 and stamp(r) is not None
+                  and self.t0 - 0.02 <= stamp(r) <= self.t1 + 0.02]
+        use = inside or rows
+        num = lambda x: x.replace(".", "", 1).isdigit()
+        sm = [float(r[2]) for r in use if len(r) > 2 and num(r[2])]
+        mx = [float(r[3]) for r in use if len(r) > 3 and num(r[3])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[j] for r in rows for j in range(4) if len(r) > 5 + j and r[5 + j].strip() == "Active"})
+        reasons = sorted({names[j] for r in use for j in range(4) if len(r) > 6 + j and r[6 + j].strip() == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(use), "samples_in_timed_region": len(inside),
+                "interval_ms": 20}
 
 
 # ------------------------------------------------------------------ oracle error
@@ -222,7 +247,8 @@ def extra_configs(args, dev, flush):
     idx2 = np.arange(0, B2, B2 // 256)
     ref2, _ = oracle.vern9("robertson", u02[idx2].astype(np.float64), k[idx2].astype(np.float64), 0.0, np.array([1e5]),
                            rtol=1e-10, atol=1e-14, method="rodas5p")
-    for name, alg in (("rosenbrock23", degpu.GPURosenbrock23()), ("rodas5p", degpu.GPURodas5P())):
+    for name, alg in (("rosenbrock23", degpu.GPURosenbrock23()), ("rodas5p", degpu.GPURodas5P()),
+                      ("rodas4", degpu.GPURodas4())):
         def run2():
             holder["r"] = degpu.api._solve_device(pr2, alg, True, dt=1e-3, saveat=sa2, abstol=1e-7, reltol=1e-4)
         ms = time_solve(run2)
@@ -395,11 +421,13 @@ def gpu_arm(args):
         dist.barrier()
     with ClockSampler(local) as clk:
         torch.cuda.synchronize(dev)
+        clk.mark(True)
         wall0 = time.perf_counter()
         t_plain = timed_steps(plain_launch, args.steps, stream, flush)
         t_lrn = timed_steps(lambda: lrn["graph"].replay(), args.steps, stream, flush) if lrn else None
         torch.cuda.synchronize(dev)
         wall = time.perf_counter() - wall0
+        clk.mark(False)
 
     def agg(times):
         tot = float(np.sum(times))

@@ -364,7 +364,7 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   if (!f || !pr || !o || !out) return fail(DEGPU_E_INVALID, "null argument");
   if (pr->B < 0) return fail(DEGPU_E_INVALID, "negative trajectory count");
   if (pr->B > 0x7fffffffLL) return fail(DEGPU_E_INVALID, "more than 2^31-1 trajectories in one call; split into batches");
-  if (o->alg < 0 || o->alg > 4) return fail(DEGPU_E_INVALID, "unknown algorithm");
+  if (o->alg < 0 || o->alg > 5) return fail(DEGPU_E_INVALID, "unknown algorithm");
   if (o->alg == DEGPU_ALG_EM && adaptive)
     return fail(DEGPU_E_UNSUPPORTED, "Adaptive time-stepping is not supported yet with GPUEM.");
   if (o->alg == DEGPU_ALG_EM && !(f->flags & DEGPU_RHS_HAS_NOISE))
@@ -394,8 +394,9 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   else if (o->jac == DEGPU_JAC_AD) { k.jac = 0; k.tgrad = 0; }
   else if (o->jac == DEGPU_JAC_FINITEDIFF) { k.jac = 2; k.tgrad = 2; }
   else return fail(DEGPU_E_INVALID, "jac");
-  if (o->alg != DEGPU_ALG_ROSENBROCK23 && o->alg != DEGPU_ALG_RODAS5P) { k.jac = 0; k.tgrad = 0; }
-  k.refine = (o->alg == DEGPU_ALG_ROSENBROCK23 || o->alg == DEGPU_ALG_RODAS5P) && !k.parity ? 1 : 0;
+  const bool rosenbrock = o->alg == DEGPU_ALG_ROSENBROCK23 || o->alg == DEGPU_ALG_RODAS5P || o->alg == DEGPU_ALG_RODAS4;
+  if (!rosenbrock) { k.jac = 0; k.tgrad = 0; }
+  k.refine = rosenbrock && !k.parity ? 1 : 0;
   degpu_kparams& P = rq->kp;
   memset(&P, 0, sizeof P);
   P.u0 = pr->u0;

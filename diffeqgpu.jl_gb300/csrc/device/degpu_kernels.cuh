@@ -5,7 +5,7 @@
 // defines, per translation unit:
 //   DEGPU_N, DEGPU_P        state / parameter dimensions
 //   DEGPU_TT                time type (float: the reference's Float32 tspan; double: FP64 time)
-//   DEGPU_ALG               0 Tsit5, 1 Vern7, 2 Rosenbrock23, 3 Rodas5P, 4 EM
+//   DEGPU_ALG               0 Tsit5, 1 Vern7, 2 Rosenbrock23, 3 Rodas5P, 4 EM, 5 Rodas4
 //   DEGPU_DRIVER            0 fixed step, 1 adaptive (one trajectory per thread),
 //                           2 adaptive persistent (warp refill + work stealing), 3 EM
 //   DEGPU_PARITY            1: no FMA (set by --fmad=false), portable pow, Cramer solves
@@ -107,6 +107,9 @@ constexpr int ORDER = 2;
 #elif DEGPU_ALG == 3
 constexpr int NK = 3;
 constexpr int ORDER = 5;
+#elif DEGPU_ALG == 5
+constexpr int NK = 2;
+constexpr int ORDER = 4;
 #else
 constexpr int NK = 1;
 constexpr int ORDER = 1;
@@ -147,6 +150,7 @@ __constant__ float c_tsit5[TS_COUNT] = {
 #define V7X(n) c_vern7x[VERN7X_##n]
 #define V7I(n) c_vern7i[VERN7I_##n]
 #define RP(n) c_rodas5p[RODAS5P_##n]
+#define R4(n) c_rodas4[RODAS4_##n]
 
 // ------------------------------------------------------------------ small helpers
 DEGPU_DEV float tstage(Time t, float c, float dt) { return TP::stage(t, c, dt); }
@@ -384,7 +388,7 @@ struct LinSys {
 struct Lane {
   float u[N], uprev[N];
   float k[NK][N];
-#if DEGPU_ALG == 2 || DEGPU_ALG == 3
+#if DEGPU_ALG == 2 || DEGPU_ALG == 3 || DEGPU_ALG == 5
   float J[N * N], dT[N];
 #endif
 #if DEGPU_ALG == 2
@@ -719,7 +723,90 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 }
 #endif
 
-#if DEGPU_ALG <= 3
+// ------------------------------------------------------------------ Rodas4 (gpu_rodas4_perform_step.jl)
+#if DEGPU_ALG == 5
+DEGPU_DEV void begin_step(Lane& L, bool) {
+  float tf_ = TP::f32(L.t);  // J, dT once per step, outside the reject loop (:145-149)
+  jacobian(L.J, L.uprev, L.p, tf_);
+  tgrad(L.dT, L.uprev, L.p, tf_);
+}
+template <bool ADAPTIVE>
+DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* uout, float* err) {
+  const float* up = L.uprev;
+  float dtC21 = R4(C21) / dt, dtC31 = R4(C31) / dt, dtC32 = R4(C32) / dt, dtC41 = R4(C41) / dt, dtC42 = R4(C42) / dt, dtC43 = R4(C43) / dt;
+  float dtC51 = R4(C51) / dt, dtC52 = R4(C52) / dt, dtC53 = R4(C53) / dt, dtC54 = R4(C54) / dt;
+  float dtC61 = R4(C61) / dt, dtC62 = R4(C62) / dt, dtC63 = R4(C63) / dt, dtC64 = R4(C64) / dt, dtC65 = R4(C65) / dt;
+  float dtd1 = dt * R4(d1), dtd2 = dt * R4(d2), dtd3 = dt * R4(d3), dtd4 = dt * R4(d4);
+  float dtgamma = dt * R4(gamma);
+  float inv_dtg = 1.0f / dtgamma;
+  LinSys S;
+#pragma unroll
+  for (int j = 0; j < N; j++)
+#pragma unroll
+    for (int i = 0; i < N; i++) S.W[i + N * j] = L.J[i + N * j] - (i == j ? 1.0f : 0.0f) * inv_dtg;
+#if !(DEGPU_PARITY || DEGPU_N > 3)
+  S.factor();
+#endif
+  float du[N], u[N], lt[N];
+  float k1[N], k2[N], k3[N], k4[N], k5[N], k6[N];
+#define SOLVE(K)                                  \
+  {                                               \
+    _Pragma("unroll") for (int i = 0; i < N; i++) lt[i] = -lt[i]; \
+    S.solve(lt, K);                               \
+  }
+  rhs(du, up, L.p, TP::f32(t));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd1 * L.dT[i];
+  SOLVE(k1);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + R4(a21) * k1[i];
+  rhs(du, u, L.p, tstage(t, R4(c2), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd2 * L.dT[i] + dtC21 * k1[i];
+  SOLVE(k2);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + R4(a31) * k1[i] + R4(a32) * k2[i];
+  rhs(du, u, L.p, tstage(t, R4(c3), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd3 * L.dT[i] + (dtC31 * k1[i] + dtC32 * k2[i]);
+  SOLVE(k3);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + R4(a41) * k1[i] + R4(a42) * k2[i] + R4(a43) * k3[i];
+  rhs(du, u, L.p, tstage(t, R4(c4), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd4 * L.dT[i] + (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]);
+  SOLVE(k4);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + R4(a51) * k1[i] + R4(a52) * k2[i] + R4(a53) * k3[i] + R4(a54) * k4[i];
+  rhs(du, u, L.p, tstage(t, 1.0f, dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]);
+  SOLVE(k5);
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = u[i] + k5[i];
+  rhs(du, u, L.p, tstage(t, 1.0f, dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC65 * k5[i] + dtC64 * k4[i] + dtC63 * k3[i]);
+  SOLVE(k6);
+#undef SOLVE
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    uout[i] = u[i] + k6[i];
+    err[i] = k6[i];  // the error estimate is k6 (:226-227)
+    // dense-output vectors (:107-108, :246-247), consumed only after an accept
+    L.k[0][i] = R4(h21) * k1[i] + R4(h22) * k2[i] + R4(h23) * k3[i] + R4(h24) * k4[i] + R4(h25) * k5[i];
+    L.k[1][i] = R4(h31) * k1[i] + R4(h32) * k2[i] + R4(h33) * k3[i] + R4(h34) * k4[i] + R4(h35) * k5[i];
+  }
+}
+// stiff/interpolants.jl:1-11
+DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
+  float th1 = 1.0f - th;
+#pragma unroll
+  for (int i = 0; i < N; i++) out[i] = th1 * L.uprev[i] + th * (L.u[i] + th1 * (L.k[0][i] + th * L.k[1][i]));
+}
+#endif
+
+#if DEGPU_ALG <= 3 || DEGPU_ALG == 5
 // ------------------------------------------------------------------ driver pieces (kernels.jl)
 // Loop-invariant kernel parameters copied into registers once per thread (reading them
 // through a reference to the parameter block inside the step loop costs a constant-bank
@@ -1214,7 +1301,7 @@ DEGPU_DEV void lane_finish(Lane& L, const Io& io, int i) {
   if (io.P.naccept) io.P.naccept[i] = L.naccept;
   if (io.P.nreject) io.P.nreject[i] = L.nreject;
 }
-#endif  // DEGPU_ALG <= 3
+#endif  // DEGPU_ALG <= 3 || DEGPU_ALG == 5
 
 }  // namespace degpu
 

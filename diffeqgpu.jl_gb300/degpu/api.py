@@ -70,6 +70,10 @@ class GPURodas5P(GPUODEImplicitAlgorithm):
     alg_id, order = _lib.ALG_RODAS5P, 5
 
 
+class GPURodas4(GPUODEImplicitAlgorithm):
+    alg_id, order = _lib.ALG_RODAS4, 4
+
+
 # The reference has no Rodas5 (non-P) tableau; GPURodas5 is Rodas5P's coefficients.
 GPURodas5 = GPURodas5P
 

@@ -42,6 +42,10 @@ def attempt_flops(alg: str, N: int, model: str, adaptive: bool = True) -> int:
         lu = 2 * N ** 3 // 3 + N * N
         solve = 2 * N * N
         return 28 + 6 + N * N + lu + 8 * solve + 8 * rhs + 120 * N + (5 * N + 14 if adaptive else 0)
+    if alg == "rodas4":
+        lu = 2 * N ** 3 // 3 + N * N
+        solve = 2 * N * N
+        return 21 + N * N + lu + 6 * solve + 6 * rhs + 78 * N + (5 * N + 14 if adaptive else 0)
     raise ValueError(alg)
 
 
@@ -50,7 +54,7 @@ def step_flops(alg: str, N: int, model: str) -> int:
     rhs = RHS_FLOPS[model]
     if alg == "vern7":
         return rhs
-    if alg in ("rosenbrock23", "rodas5p"):
+    if alg in ("rosenbrock23", "rodas5p", "rodas4"):
         return 3 * rhs * N  # Jacobian by forward-mode AD ~ N dual sweeps
     return 0
 
@@ -63,6 +67,8 @@ def interp_flops(alg: str, N: int, model: str) -> int:
         return 13 * 12 + 6 * rhs + (2 * 9 + 1) * 6 * N + 30 * N
     if alg == "rosenbrock23":
         return 8 + 5 * N
+    if alg == "rodas4":
+        return 1 + 7 * N
     return 8 + 9 * N
 
 

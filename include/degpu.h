@@ -30,13 +30,14 @@ extern "C" {
 #define DEGPU_E_CUDA (-3)      /* CUDA driver/runtime error */
 #define DEGPU_E_UNSUPPORTED (-4) /* combination the reference also rejects */
 
-/* algorithms: GPUTsit5, GPUVern7, GPURosenbrock23, GPURodas5P (alias GPURodas5), GPUEM
- * (src/ensemblegpukernel/gpukernel_algorithms.jl:30, 57, 112, 162, 243) */
+/* algorithms: GPUTsit5, GPUVern7, GPURosenbrock23, GPURodas5P (alias GPURodas5), GPUEM,
+ * GPURodas4 (src/ensemblegpukernel/gpukernel_algorithms.jl:30, 57, 112, 162, 243, 137) */
 #define DEGPU_ALG_TSIT5 0
 #define DEGPU_ALG_VERN7 1
 #define DEGPU_ALG_ROSENBROCK23 2
 #define DEGPU_ALG_RODAS5P 3
 #define DEGPU_ALG_EM 4
+#define DEGPU_ALG_RODAS4 5 /* GPURodas4 (gpukernel_algorithms.jl:137, perform_step/gpu_rodas4_perform_step.jl) */
 
 #define DEGPU_TIME_F32 0 /* Float32 tspan: every operation is the reference's Float32 one */
 #define DEGPU_TIME_F64 1 /* FP64 time accumulation / end detection, FP32 state */

@@ -8,7 +8,8 @@ Test-infrastructure / build-time recipe.  It reads the reference's tableau sourc
   * ``diffeqgpu.jl_gb300/csrc/device/tableaus_gen.cuh`` -- FP32 ``__constant__`` arrays for
     the kernels.
 
-The reference writes every coefficient as ``name = convert(T, <Float64 literal>)``
+The reference writes every coefficient as ``name = convert(T, <Float64 literal>)`` (or
+its negation ``-convert(T, ...)``)
 (``src/ensemblegpukernel/tableaus/verner_tableaus.jl`` and ``rodas_tableaus.jl``) and
 Julia's ``convert(Float32, x::Float64)`` rounds to nearest.  The device header stores
 ``float(np.float32(np.float64(literal)))`` printed with enough digits to round-trip,
@@ -33,9 +34,10 @@ TABLES = [
     ("vern7i", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern7InterpolationCoefficients"),
     ("vern9", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern9Tableau"),
     ("rodas5p", "src/ensemblegpukernel/tableaus/rodas_tableaus.jl", "Rodas5PTableau"),
+    ("rodas4", "src/ensemblegpukernel/tableaus/rodas_tableaus.jl", "Rodas4Tableau"),
 ]
 
-ASSIGN = re.compile(r"^\s*([A-Za-z_γ][A-Za-z0-9_γ]*)\s*=\s*convert\(\s*T2?\s*,\s*([-+0-9.eE]+)\s*\)\s*$")
+ASSIGN = re.compile(r"^\s*([A-Za-z_γ][A-Za-z0-9_γ]*)\s*=\s*(-?)\s*convert\(\s*T2?\s*,\s*([-+0-9.eE]+)\s*\)\s*$")
 
 
 def parse_function(path: Path, fname: str):
@@ -57,7 +59,8 @@ def parse_function(path: Path, fname: str):
         m = ASSIGN.match(ln)
         if m:
             name = m.group(1).replace("γ", "gamma")
-            out.append((name, float(m.group(2))))
+            v = float(m.group(3))
+            out.append((name, -v if m.group(2) else v))  # `-convert(T, x)`: negation is exact
     return out, start + 1, end + 1
 
 
@@ -80,7 +83,7 @@ def main():
     ]
     dev_lines = [
         "// Generated by oracle/gen_tableaus.py -- do not edit.",
-        "// Method coefficients (Verner 7(6), Rodas5P) rounded once from their published FP64",
+        "// Method coefficients (Verner 7(6), Rodas5P, Rodas4) rounded once from their published FP64",
         "// values to FP32, exactly as Julia's convert(Float32, ::Float64) does in the reference",
         "// (see per-table citations).  They live in constant memory and are read as",
         "// constant-bank operands by the stage arithmetic.",

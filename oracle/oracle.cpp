@@ -52,7 +52,7 @@
 #include "tableaus_gen.h"
 
 /* ------------------------------------------------------------------ constants */
-enum { ALG_TSIT5 = 0, ALG_VERN7 = 1, ALG_RB23 = 2, ALG_RODAS5P = 3, ALG_EM = 4 };
+enum { ALG_TSIT5 = 0, ALG_VERN7 = 1, ALG_RB23 = 2, ALG_RODAS5P = 3, ALG_EM = 4, ALG_RODAS4 = 5 };
 enum { RET_DEFAULT = 0, RET_SUCCESS = 1, RET_TERMINATED = 2, RET_DTMIN = 3, RET_MAXITERS = 4, RET_UNSTABLE = 5 };
 enum { JAC_AD = 0, JAC_ANALYTIC = 1, JAC_FINITEDIFF = 2 };
 enum {
@@ -311,7 +311,7 @@ static Tsit5Tab make_tsit5() {
 }
 static const Tsit5Tab TS5 = make_tsit5();
 
-static float V7[OR_VERN7_COUNT], V7X[OR_VERN7X_COUNT], V7I[OR_VERN7I_COUNT], R5P[OR_RODAS5P_COUNT];
+static float V7[OR_VERN7_COUNT], V7X[OR_VERN7X_COUNT], V7I[OR_VERN7I_COUNT], R5P[OR_RODAS5P_COUNT], R4T[OR_RODAS4_COUNT];
 static int tabs_ready = 0;
 static void init_tabs() {
   if (tabs_ready) return;
@@ -322,6 +322,7 @@ static void init_tabs() {
       for (int i = 0; i < OR_VERN7X_COUNT; i++) V7X[i] = (float)OR_VERN7X[i];
       for (int i = 0; i < OR_VERN7I_COUNT; i++) V7I[i] = (float)OR_VERN7I[i];
       for (int i = 0; i < OR_RODAS5P_COUNT; i++) R5P[i] = (float)OR_RODAS5P[i];
+      for (int i = 0; i < OR_RODAS4_COUNT; i++) R4T[i] = (float)OR_RODAS4[i];
       tabs_ready = 1;
     }
   }
@@ -330,6 +331,7 @@ static void init_tabs() {
 #define V7XC(n) V7X[OR_VERN7X_##n]
 #define V7IC(n) V7I[OR_VERN7I_##n]
 #define RPC(n) R5P[OR_RODAS5P_##n]
+#define R4C(n) R4T[OR_RODAS4_##n]
 
 /* ------------------------------------------------------------------ configuration */
 extern "C" {
@@ -565,7 +567,9 @@ static Ctrl make_ctrl(int order) {
   c.qmax = 10.0f; c.qmin = (float)(1.0 / 5.0); c.gamma = (float)(9.0 / 10.0); c.qoldinit = (float)1.0e-4;
   return c;
 }
-static int alg_order(int alg) { return alg == ALG_TSIT5 ? 5 : alg == ALG_VERN7 ? 7 : alg == ALG_RB23 ? 2 : alg == ALG_RODAS5P ? 5 : 1; }
+static int alg_order(int alg) {
+  return alg == ALG_TSIT5 ? 5 : alg == ALG_VERN7 ? 7 : alg == ALG_RB23 ? 2 : alg == ALG_RODAS5P ? 5 : alg == ALG_RODAS4 ? 4 : 1;
+}
 
 /* PI controller decision, shared by every adaptive step! (e.g. gpu_tsit5_perform_step.jl:124-170).
  * Returns 1 if accepted; updates dt (reject) or dt_accepted/dtnew/qold (accept). */
@@ -685,6 +689,56 @@ static void rodas5p_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt
   }
 }
 
+/* ------------------------------------------------------------------ Rodas4
+ * gpu_rodas4_perform_step.jl:1-114 (fixed) / :116-277 (adaptive): 6 stages, error estimate
+ * k6, two dense-output vectors; J and dT once per step (:36-40, :145-149). */
+template <class Tt>
+static void rodas4_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt, float* uout, float* k6o, float (*dense)[MAXN]) {
+  int N = ig.N;
+  const float* J = ig.J; const float* dT = ig.dT; const float* up = ig.uprev;
+  float dtC21 = R4C(C21) / dt, dtC31 = R4C(C31) / dt, dtC32 = R4C(C32) / dt, dtC41 = R4C(C41) / dt, dtC42 = R4C(C42) / dt, dtC43 = R4C(C43) / dt;
+  float dtC51 = R4C(C51) / dt, dtC52 = R4C(C52) / dt, dtC53 = R4C(C53) / dt, dtC54 = R4C(C54) / dt;
+  float dtC61 = R4C(C61) / dt, dtC62 = R4C(C62) / dt, dtC63 = R4C(C63) / dt, dtC64 = R4C(C64) / dt, dtC65 = R4C(C65) / dt;
+  float dtd1 = dt * R4C(d1), dtd2 = dt * R4C(d2), dtd3 = dt * R4C(d3), dtd4 = dt * R4C(d4);
+  float dtgamma = dt * R4C(gamma);
+  float W[MAXN * MAXN];
+  float inv_dtg = 1.0f / dtgamma;
+  for (int j = 0; j < N; j++) for (int i = 0; i < N; i++) W[i + N * j] = J[i + N * j] - (i == j ? 1.0f : 0.0f) * inv_dtg;
+  float du[MAXN], u[MAXN], lt[MAXN], neg[MAXN];
+  float k1[MAXN], k2[MAXN], k3[MAXN], k4[MAXN], k5[MAXN], k6[MAXN];
+  float tf_ = t_f32(t);
+#define SOLVE(K) { for (int i = 0; i < N; i++) neg[i] = -lt[i]; linear_solve(N, W, neg, K); }
+  model_f<float>(m, du, up, p, tf_);
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd1 * dT[i];
+  SOLVE(k1);
+  for (int i = 0; i < N; i++) u[i] = up[i] + R4C(a21) * k1[i];
+  model_f<float>(m, du, u, p, tstage(t, R4C(c2), dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd2 * dT[i] + dtC21 * k1[i];
+  SOLVE(k2);
+  for (int i = 0; i < N; i++) u[i] = up[i] + R4C(a31) * k1[i] + R4C(a32) * k2[i];
+  model_f<float>(m, du, u, p, tstage(t, R4C(c3), dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd3 * dT[i] + (dtC31 * k1[i] + dtC32 * k2[i]);
+  SOLVE(k3);
+  for (int i = 0; i < N; i++) u[i] = up[i] + R4C(a41) * k1[i] + R4C(a42) * k2[i] + R4C(a43) * k3[i];
+  model_f<float>(m, du, u, p, tstage(t, R4C(c4), dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd4 * dT[i] + (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]);
+  SOLVE(k4);
+  for (int i = 0; i < N; i++) u[i] = up[i] + R4C(a51) * k1[i] + R4C(a52) * k2[i] + R4C(a53) * k3[i] + R4C(a54) * k4[i];
+  model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]);
+  SOLVE(k5);
+  for (int i = 0; i < N; i++) u[i] = u[i] + k5[i];
+  model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
+  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC65 * k5[i] + dtC64 * k4[i] + dtC63 * k3[i]);
+  SOLVE(k6);
+#undef SOLVE
+  for (int i = 0; i < N; i++) { uout[i] = u[i] + k6[i]; k6o[i] = k6[i]; }
+  for (int i = 0; i < N; i++) {
+    dense[0][i] = R4C(h21) * k1[i] + R4C(h22) * k2[i] + R4C(h23) * k3[i] + R4C(h24) * k4[i] + R4C(h25) * k5[i];
+    dense[1][i] = R4C(h31) * k1[i] + R4C(h32) * k2[i] + R4C(h33) * k3[i] + R4C(h34) * k4[i] + R4C(h35) * k5[i];
+  }
+}
+
 /* ------------------------------------------------------------------ interpolation (savevalues!) */
 template <class Tt>
 static void interpolate(int m, int alg, const Integ<Tt>& ig, const float* p, float th, float dt, float* out) {
@@ -703,6 +757,10 @@ static void interpolate(int m, int alg, const Integ<Tt>& ig, const float* p, flo
       float c1 = th * (1.0f - th) / (1.0f - 2.0f * d);
       float c2 = th * (th - 2.0f * d) / (1.0f - 2.0f * d);
       for (int i = 0; i < N; i++) out[i] = y0[i] + dt * (c1 * ig.k[0][i] + c2 * ig.k[1][i]);
+    } break;
+    case ALG_RODAS4: { /* stiff/interpolants.jl:1-11 */
+      float th1 = 1.0f - th;
+      for (int i = 0; i < N; i++) out[i] = th1 * y0[i] + th * (ig.u[i] + th1 * (ig.k[0][i] + th * ig.k[1][i]));
     } break;
     case ALG_RODAS5P: { /* stiff/interpolants.jl:13-23 */
       float th1 = 1.0f - th;
@@ -966,6 +1024,11 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
         compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, t_f32(t));
         compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, t_f32(t));
         rodas5p_attempt(m, ig, p, t, dt, u, k8, ig.k);
+      } else if (alg == ALG_RODAS4) {
+        float k6[MAXN];
+        compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, t_f32(t));
+        compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, t_f32(t));
+        rodas4_attempt(m, ig, p, t, dt, u, k6, ig.k);
       }
       for (int i = 0; i < N; i++) ig.u[i] = u[i];
       ig.naccept++;
@@ -976,7 +1039,7 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
         if (ig.u_modified) { model_f<float>(m, k1, ig.uprev, p, t_f32(t)); ig.u_modified = 0; }
         else for (int i = 0; i < N; i++) k1[i] = ig.k[6][i];
       }
-      if (alg == ALG_RODAS5P) { /* J, dT once per step, outside the reject loop (:182-186) */
+      if (alg == ALG_RODAS5P || alg == ALG_RODAS4) { /* J, dT once per step, outside the reject loop */
         compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, t_f32(t));
         compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, t_f32(t));
       }
@@ -995,12 +1058,14 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
             err[i] = dt * (V7C(btilde1) * kk[0][i] + V7C(btilde4) * kk[3][i] + V7C(btilde5) * kk[4][i] + V7C(btilde6) * kk[5][i] + V7C(btilde7) * kk[6][i] + V7C(btilde8) * kk[7][i] + V7C(btilde9) * kk[8][i] + V7C(btilde10) * kk[9][i]);
         } else if (alg == ALG_RB23) {
           rb23_attempt(m, cfg->jac, ig, p, t, dt, u, kk[0], kk[1], err, 1);
+        } else if (alg == ALG_RODAS4) { /* error estimate is k6 */
+          rodas4_attempt(m, ig, p, t, dt, u, err, kk);
         } else { /* Rodas5P: error estimate is k8 */
           rodas5p_attempt(m, ig, p, t, dt, u, err, kk);
         }
         EEst = scaled_norm(err, ig.uprev, u, N, ig.abstol, ig.reltol);
         if (controller(ig, C, EEst, dt, t)) {
-          int ns = alg == ALG_TSIT5 ? 7 : alg == ALG_VERN7 ? 10 : alg == ALG_RB23 ? 2 : 3;
+          int ns = alg == ALG_TSIT5 ? 7 : alg == ALG_VERN7 ? 10 : (alg == ALG_RB23 || alg == ALG_RODAS4) ? 2 : 3;
           for (int s = 0; s < ns; s++) for (int i = 0; i < N; i++) ig.k[s][i] = kk[s][i];
           for (int i = 0; i < N; i++) ig.u[i] = u[i];
           /* not snapped to tf: stop at the next tstop, u = integ(tstop) (:157-167) */

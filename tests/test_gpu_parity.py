@@ -13,7 +13,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-ALGS = {"tsit5": "GPUTsit5", "vern7": "GPUVern7", "rosenbrock23": "GPURosenbrock23", "rodas5p": "GPURodas5P"}
+ALGS = {"tsit5": "GPUTsit5", "vern7": "GPUVern7", "rosenbrock23": "GPURosenbrock23", "rodas5p": "GPURodas5P",
+        "rodas4": "GPURodas4"}
 
 
 def lorenz_batch(B, seed=0, chaotic=True):
@@ -90,7 +91,7 @@ def test_fixed_step_save_everystep_parity(degpu_mod, oracle_mod):
     assert_bit_equal(ts, ots, "ts")
 
 
-@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p"])
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p", "rodas4"])
 def test_fixed_step_saveat_parity(degpu_mod, oracle_mod, alg):
     u0, p = lorenz_batch(300, seed=3, chaotic=False)
     sa = np.array([0.0, 0.25, 2.0, 4.0, 5.05, 10.0], np.float32)
@@ -135,7 +136,7 @@ def test_adaptive_saveat_bit_parity(degpu_mod, oracle_mod, alg, driver, tt):
     assert_bit_equal(ts, ots, "ts")
 
 
-@pytest.mark.parametrize("alg", ["rosenbrock23", "rodas5p"])
+@pytest.mark.parametrize("alg", ["rosenbrock23", "rodas5p", "rodas4"])
 @pytest.mark.parametrize("jac", ["auto", "ad", "finitediff"])
 def test_stiff_robertson_bit_parity(degpu_mod, oracle_mod, alg, jac):
     """Robertson kinetics, k scaled by lognormal(0,0.3), tspan (0,1e5), 32 log-spaced
@@ -152,7 +153,7 @@ def test_stiff_robertson_bit_parity(degpu_mod, oracle_mod, alg, jac):
     assert_saved_equal(us, ous, ots, 0.0)
 
 
-@pytest.mark.parametrize("alg", ["rosenbrock23", "rodas5p"])
+@pytest.mark.parametrize("alg", ["rosenbrock23", "rodas5p", "rodas4"])
 def test_stiff_fast_mode_vs_fp64(degpu_mod, oracle_mod, alg):
     """Fast mode (pivoted LU + compensated residual refinement) against the FP64 stiff
     oracle: final-state relative error of the dominant species within 10x reltol."""
