@@ -283,6 +283,23 @@ def extra_configs(args, dev, flush):
     out3["persistent_speedup"] = out3["persistent"]["trajectories_per_s"] / out3["naive"]["trajectories_per_s"]
     res[f"uneven_lorenz_{B3}"] = out3
 
+    # the adaptive Lorenz ensemble with GPUVern9 at tight tolerances (reltol 1e-8, abstol 1e-10)
+    B5 = 1 << 20
+    u05, p05 = make_inputs(B5, WORKLOAD["seed"] + 5)
+    pr5 = degpu.DeviceProblems(f, u05, p05, np.tile(np.array(WORKLOAD["tspan"], np.float64), (B5, 1)), np.float64, dev)
+    sa5 = saveat_grid()
+
+    def run5():
+        holder["r"] = degpu.api._solve_device(pr5, degpu.GPUVern9(), True, dt=0.1, saveat=sa5, abstol=1e-10,
+                                              reltol=1e-8)
+    ms = time_solve(run5)
+    r = holder["r"]
+    na, nr = r.naccept.cpu().numpy(), r.nreject.cpu().numpy()
+    fl = flops.solve_flops("vern9", 3, "lorenz", na, nr, nsaves=B5 * len(sa5))
+    res["lorenz_vern9_1M_reltol1e-8"] = {
+        "trajectories_per_s": B5 / (ms * 1e-3), "ms": ms, "attempts_per_traj": float((na + nr).mean()),
+        "fp32_tflops": fl / (ms * 1e-3) / 1e12, "retcodes_ok": bool((r.retcode.cpu().numpy() == 1).all())}
+
     # bouncing balls with a continuous callback (ITP event location + affect): heights
     # U(5, 50), gravities U(5, 15), tspan (0, 12), 25 saved points, error against the exact bounce
     B4 = 1 << 20

@@ -100,7 +100,7 @@ def compile_lib(verbose: bool = False) -> Path:
 CHECKS = [  # (alg, driver, time type, parity, model, extra defines) compiled by the build check
     (0, 0, "float", 1, "lorenz", ""), (0, 1, "double", 0, "lorenz", ""), (0, 2, "double", 0, "lorenz", ""),
     (1, 2, "double", 0, "lorenz", ""), (2, 2, "double", 0, "lorenz", ""), (3, 2, "double", 0, "lorenz", ""),
-    (3, 1, "double", 1, "lorenz", ""),
+    (3, 1, "double", 1, "lorenz", ""), (5, 2, "double", 0, "lorenz", ""), (6, 2, "double", 0, "lorenz", ""),
     # tstops + callbacks: continuous (bouncing ball) and discrete (decay) sets
     (0, 2, "double", 0, "ball", "-DDEGPU_NCCB=2 -DDEGPU_TSTOPS=1"),
     (1, 0, "float", 1, "decay", "-DDEGPU_NDCB=2 -DDEGPU_TSTOPS=1"),

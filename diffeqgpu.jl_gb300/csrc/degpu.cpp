@@ -364,7 +364,7 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   if (!f || !pr || !o || !out) return fail(DEGPU_E_INVALID, "null argument");
   if (pr->B < 0) return fail(DEGPU_E_INVALID, "negative trajectory count");
   if (pr->B > 0x7fffffffLL) return fail(DEGPU_E_INVALID, "more than 2^31-1 trajectories in one call; split into batches");
-  if (o->alg < 0 || o->alg > 5) return fail(DEGPU_E_INVALID, "unknown algorithm");
+  if (o->alg < 0 || o->alg > 6) return fail(DEGPU_E_INVALID, "unknown algorithm");
   if (o->alg == DEGPU_ALG_EM && adaptive)
     return fail(DEGPU_E_UNSUPPORTED, "Adaptive time-stepping is not supported yet with GPUEM.");
   if (o->alg == DEGPU_ALG_EM && !(f->flags & DEGPU_RHS_HAS_NOISE))

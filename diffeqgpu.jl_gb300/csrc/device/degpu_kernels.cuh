@@ -5,7 +5,7 @@
 // defines, per translation unit:
 //   DEGPU_N, DEGPU_P        state / parameter dimensions
 //   DEGPU_TT                time type (float: the reference's Float32 tspan; double: FP64 time)
-//   DEGPU_ALG               0 Tsit5, 1 Vern7, 2 Rosenbrock23, 3 Rodas5P, 4 EM, 5 Rodas4
+//   DEGPU_ALG               0 Tsit5, 1 Vern7, 2 Rosenbrock23, 3 Rodas5P, 4 EM, 5 Rodas4, 6 Vern9
 //   DEGPU_DRIVER            0 fixed step, 1 adaptive (one trajectory per thread),
 //                           2 adaptive persistent (warp refill + work stealing), 3 EM
 //   DEGPU_PARITY            1: no FMA (set by --fmad=false), portable pow, Cramer solves
@@ -110,6 +110,9 @@ constexpr int ORDER = 5;
 #elif DEGPU_ALG == 5
 constexpr int NK = 2;
 constexpr int ORDER = 4;
+#elif DEGPU_ALG == 6
+constexpr int NK = 10;
+constexpr int ORDER = 9;
 #else
 constexpr int NK = 1;
 constexpr int ORDER = 1;
@@ -151,6 +154,9 @@ __constant__ float c_tsit5[TS_COUNT] = {
 #define V7I(n) c_vern7i[VERN7I_##n]
 #define RP(n) c_rodas5p[RODAS5P_##n]
 #define R4(n) c_rodas4[RODAS4_##n]
+#define V9(n) c_vern9[VERN9_##n]
+#define V9X(n) c_vern9x[VERN9X_##n]
+#define V9I(n) c_vern9i[VERN9I_##n]
 
 // ------------------------------------------------------------------ small helpers
 DEGPU_DEV float tstage(Time t, float c, float dt) { return TP::stage(t, c, dt); }
@@ -806,7 +812,307 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 }
 #endif
 
-#if DEGPU_ALG <= 3 || DEGPU_ALG == 5
+// ------------------------------------------------------------------ Vern9 (gpu_vern9_perform_step.jl)
+// 16 stages, 9(8) pair; L.k holds k1, k8..k16 (the stages the error estimate and the dense
+// output use), k2..k7 live only inside the attempt.  Dense output: 10 extra stages and the
+// degree-9 polynomials bΘs (nonstiff/interpolants.jl:192-371), k16 unused there.
+#if DEGPU_ALG == 6
+DEGPU_DEV void begin_step(Lane& L, bool) {
+  // not FSAL: k1 = f(uprev, p, t) every step (:33, :170; one evaluation per step suffices)
+  rhs(L.k[0], L.uprev, L.p, TP::f32(L.t));
+}
+template <bool ADAPTIVE>
+DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
+  float tmp[N], k2[N], k3[N], k4[N], k5[N], k6[N], k7[N];
+  const float* up = L.uprev;
+  float(*k)[N] = L.k;
+  float a = dt * V9(a0201);
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + a * k[0][i];
+  rhs(k2, tmp, L.p, tstage(t, V9(c1), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a0301) * k[0][i] + V9(a0302) * k2[i]);
+  rhs(k3, tmp, L.p, tstage(t, V9(c2), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a0401) * k[0][i] + V9(a0403) * k3[i]);
+  rhs(k4, tmp, L.p, tstage(t, V9(c3), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a0501) * k[0][i] + V9(a0503) * k3[i] + V9(a0504) * k4[i]);
+  rhs(k5, tmp, L.p, tstage(t, V9(c4), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a0601) * k[0][i] + V9(a0604) * k4[i] + V9(a0605) * k5[i]);
+  rhs(k6, tmp, L.p, tstage(t, V9(c5), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a0701) * k[0][i] + V9(a0704) * k4[i] + V9(a0705) * k5[i] + V9(a0706) * k6[i]);
+  rhs(k7, tmp, L.p, tstage(t, V9(c6), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a0801) * k[0][i] + V9(a0806) * k6[i] + V9(a0807) * k7[i]);
+  rhs(k[1], tmp, L.p, tstage(t, V9(c7), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a0901) * k[0][i] + V9(a0906) * k6[i] + V9(a0907) * k7[i] + V9(a0908) * k[1][i]);
+  rhs(k[2], tmp, L.p, tstage(t, V9(c8), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a1001) * k[0][i] + V9(a1006) * k6[i] + V9(a1007) * k7[i] + V9(a1008) * k[1][i] + V9(a1009) * k[2][i]);
+  rhs(k[3], tmp, L.p, tstage(t, V9(c9), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a1101) * k[0][i] + V9(a1106) * k6[i] + V9(a1107) * k7[i] + V9(a1108) * k[1][i] + V9(a1109) * k[2][i] + V9(a1110) * k[3][i]);
+  rhs(k[4], tmp, L.p, tstage(t, V9(c10), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a1201) * k[0][i] + V9(a1206) * k6[i] + V9(a1207) * k7[i] + V9(a1208) * k[1][i] + V9(a1209) * k[2][i] + V9(a1210) * k[3][i] + V9(a1211) * k[4][i]);
+  rhs(k[5], tmp, L.p, tstage(t, V9(c11), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a1301) * k[0][i] + V9(a1306) * k6[i] + V9(a1307) * k7[i] + V9(a1308) * k[1][i] + V9(a1309) * k[2][i] + V9(a1310) * k[3][i] + V9(a1311) * k[4][i] + V9(a1312) * k[5][i]);
+  rhs(k[6], tmp, L.p, tstage(t, V9(c12), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9(a1401) * k[0][i] + V9(a1406) * k6[i] + V9(a1407) * k7[i] + V9(a1408) * k[1][i] + V9(a1409) * k[2][i] + V9(a1410) * k[3][i] + V9(a1411) * k[4][i] + V9(a1412) * k[5][i] + V9(a1413) * k[6][i]);
+  rhs(k[7], tmp, L.p, tstage(t, V9(c13), dt));
+  float g16[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    tmp[i] = up[i] + dt * (V9(a1501) * k[0][i] + V9(a1506) * k6[i] + V9(a1507) * k7[i] + V9(a1508) * k[1][i] + V9(a1509) * k[2][i] + V9(a1510) * k[3][i] + V9(a1511) * k[4][i] + V9(a1512) * k[5][i] + V9(a1513) * k[6][i] + V9(a1514) * k[7][i]);
+    g16[i] = up[i] + dt * (V9(a1601) * k[0][i] + V9(a1606) * k6[i] + V9(a1607) * k7[i] + V9(a1608) * k[1][i] + V9(a1609) * k[2][i] + V9(a1610) * k[3][i] + V9(a1611) * k[4][i] + V9(a1612) * k[5][i] + V9(a1613) * k[6][i]);
+  }
+  rhs(k[8], tmp, L.p, tstage(t, 1.0f, dt));
+  rhs(k[9], g16, L.p, tstage(t, 1.0f, dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) u[i] = up[i] + dt * (V9(b1) * k[0][i] + V9(b8) * k[1][i] + V9(b9) * k[2][i] + V9(b10) * k[3][i] + V9(b11) * k[4][i] + V9(b12) * k[5][i] + V9(b13) * k[6][i] + V9(b14) * k[7][i] + V9(b15) * k[8][i]);
+  if (ADAPTIVE) {
+#pragma unroll
+    for (int i = 0; i < N; i++) err[i] = dt * (V9(btilde1) * k[0][i] + V9(btilde8) * k[1][i] + V9(btilde9) * k[2][i] + V9(btilde10) * k[3][i] + V9(btilde11) * k[4][i] + V9(btilde12) * k[5][i] + V9(btilde13) * k[6][i] + V9(btilde14) * k[7][i] + V9(btilde15) * k[8][i] + V9(btilde16) * k[9][i]);
+  }
+}
+// Julia's @evalpoly (Horner from the highest coefficient; no FMA in parity mode)
+DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
+  const float* up = L.uprev;
+  const float(*k)[N] = L.k;
+  const Time tp = L.tprev;
+  float tmp[N], e17[N], e18[N], e19[N], e20[N], e21[N], e22[N], e23[N], e24[N], e25[N], e26[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a1701) * k[0][i] + V9X(a1708) * k[1][i] + V9X(a1709) * k[2][i] + V9X(a1710) * k[3][i] + V9X(a1711) * k[4][i] + V9X(a1712) * k[5][i] + V9X(a1713) * k[6][i] + V9X(a1714) * k[7][i] + V9X(a1715) * k[8][i]);
+  rhs(e17, tmp, L.p, tstage(tp, V9X(c17), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a1801) * k[0][i] + V9X(a1808) * k[1][i] + V9X(a1809) * k[2][i] + V9X(a1810) * k[3][i] + V9X(a1811) * k[4][i] + V9X(a1812) * k[5][i] + V9X(a1813) * k[6][i] + V9X(a1814) * k[7][i] + V9X(a1815) * k[8][i] + V9X(a1817) * e17[i]);
+  rhs(e18, tmp, L.p, tstage(tp, V9X(c18), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a1901) * k[0][i] + V9X(a1908) * k[1][i] + V9X(a1909) * k[2][i] + V9X(a1910) * k[3][i] + V9X(a1911) * k[4][i] + V9X(a1912) * k[5][i] + V9X(a1913) * k[6][i] + V9X(a1914) * k[7][i] + V9X(a1915) * k[8][i] + V9X(a1917) * e17[i] + V9X(a1918) * e18[i]);
+  rhs(e19, tmp, L.p, tstage(tp, V9X(c19), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a2001) * k[0][i] + V9X(a2008) * k[1][i] + V9X(a2009) * k[2][i] + V9X(a2010) * k[3][i] + V9X(a2011) * k[4][i] + V9X(a2012) * k[5][i] + V9X(a2013) * k[6][i] + V9X(a2014) * k[7][i] + V9X(a2015) * k[8][i] + V9X(a2017) * e17[i] + V9X(a2018) * e18[i] + V9X(a2019) * e19[i]);
+  rhs(e20, tmp, L.p, tstage(tp, V9X(c20), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a2101) * k[0][i] + V9X(a2108) * k[1][i] + V9X(a2109) * k[2][i] + V9X(a2110) * k[3][i] + V9X(a2111) * k[4][i] + V9X(a2112) * k[5][i] + V9X(a2113) * k[6][i] + V9X(a2114) * k[7][i] + V9X(a2115) * k[8][i] + V9X(a2117) * e17[i] + V9X(a2118) * e18[i] + V9X(a2119) * e19[i] + V9X(a2120) * e20[i]);
+  rhs(e21, tmp, L.p, tstage(tp, V9X(c21), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a2201) * k[0][i] + V9X(a2208) * k[1][i] + V9X(a2209) * k[2][i] + V9X(a2210) * k[3][i] + V9X(a2211) * k[4][i] + V9X(a2212) * k[5][i] + V9X(a2213) * k[6][i] + V9X(a2214) * k[7][i] + V9X(a2215) * k[8][i] + V9X(a2217) * e17[i] + V9X(a2218) * e18[i] + V9X(a2219) * e19[i] + V9X(a2220) * e20[i] + V9X(a2221) * e21[i]);
+  rhs(e22, tmp, L.p, tstage(tp, V9X(c22), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a2301) * k[0][i] + V9X(a2308) * k[1][i] + V9X(a2309) * k[2][i] + V9X(a2310) * k[3][i] + V9X(a2311) * k[4][i] + V9X(a2312) * k[5][i] + V9X(a2313) * k[6][i] + V9X(a2314) * k[7][i] + V9X(a2315) * k[8][i] + V9X(a2317) * e17[i] + V9X(a2318) * e18[i] + V9X(a2319) * e19[i] + V9X(a2320) * e20[i] + V9X(a2321) * e21[i]);
+  rhs(e23, tmp, L.p, tstage(tp, V9X(c23), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a2401) * k[0][i] + V9X(a2408) * k[1][i] + V9X(a2409) * k[2][i] + V9X(a2410) * k[3][i] + V9X(a2411) * k[4][i] + V9X(a2412) * k[5][i] + V9X(a2413) * k[6][i] + V9X(a2414) * k[7][i] + V9X(a2415) * k[8][i] + V9X(a2417) * e17[i] + V9X(a2418) * e18[i] + V9X(a2419) * e19[i] + V9X(a2420) * e20[i] + V9X(a2421) * e21[i]);
+  rhs(e24, tmp, L.p, tstage(tp, V9X(c24), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a2501) * k[0][i] + V9X(a2508) * k[1][i] + V9X(a2509) * k[2][i] + V9X(a2510) * k[3][i] + V9X(a2511) * k[4][i] + V9X(a2512) * k[5][i] + V9X(a2513) * k[6][i] + V9X(a2514) * k[7][i] + V9X(a2515) * k[8][i] + V9X(a2517) * e17[i] + V9X(a2518) * e18[i] + V9X(a2519) * e19[i] + V9X(a2520) * e20[i] + V9X(a2521) * e21[i]);
+  rhs(e25, tmp, L.p, tstage(tp, V9X(c25), dt));
+#pragma unroll
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (V9X(a2601) * k[0][i] + V9X(a2608) * k[1][i] + V9X(a2609) * k[2][i] + V9X(a2610) * k[3][i] + V9X(a2611) * k[4][i] + V9X(a2612) * k[5][i] + V9X(a2613) * k[6][i] + V9X(a2614) * k[7][i] + V9X(a2615) * k[8][i] + V9X(a2617) * e17[i] + V9X(a2618) * e18[i] + V9X(a2619) * e19[i] + V9X(a2620) * e20[i] + V9X(a2621) * e21[i]);
+  rhs(e26, tmp, L.p, tstage(tp, V9X(c26), dt));
+  float b1 = V9I(r019);
+  b1 = th * b1 + V9I(r018);
+  b1 = th * b1 + V9I(r017);
+  b1 = th * b1 + V9I(r016);
+  b1 = th * b1 + V9I(r015);
+  b1 = th * b1 + V9I(r014);
+  b1 = th * b1 + V9I(r013);
+  b1 = th * b1 + V9I(r012);
+  b1 = th * b1 + V9I(r011);
+  b1 = th * b1 + 0.0f;
+  float b8 = V9I(r089);
+  b8 = th * b8 + V9I(r088);
+  b8 = th * b8 + V9I(r087);
+  b8 = th * b8 + V9I(r086);
+  b8 = th * b8 + V9I(r085);
+  b8 = th * b8 + V9I(r084);
+  b8 = th * b8 + V9I(r083);
+  b8 = th * b8 + V9I(r082);
+  b8 = th * b8 + 0.0f;
+  b8 = th * b8 + 0.0f;
+  float b9 = V9I(r099);
+  b9 = th * b9 + V9I(r098);
+  b9 = th * b9 + V9I(r097);
+  b9 = th * b9 + V9I(r096);
+  b9 = th * b9 + V9I(r095);
+  b9 = th * b9 + V9I(r094);
+  b9 = th * b9 + V9I(r093);
+  b9 = th * b9 + V9I(r092);
+  b9 = th * b9 + 0.0f;
+  b9 = th * b9 + 0.0f;
+  float b10 = V9I(r109);
+  b10 = th * b10 + V9I(r108);
+  b10 = th * b10 + V9I(r107);
+  b10 = th * b10 + V9I(r106);
+  b10 = th * b10 + V9I(r105);
+  b10 = th * b10 + V9I(r104);
+  b10 = th * b10 + V9I(r103);
+  b10 = th * b10 + V9I(r102);
+  b10 = th * b10 + 0.0f;
+  b10 = th * b10 + 0.0f;
+  float b11 = V9I(r119);
+  b11 = th * b11 + V9I(r118);
+  b11 = th * b11 + V9I(r117);
+  b11 = th * b11 + V9I(r116);
+  b11 = th * b11 + V9I(r115);
+  b11 = th * b11 + V9I(r114);
+  b11 = th * b11 + V9I(r113);
+  b11 = th * b11 + V9I(r112);
+  b11 = th * b11 + 0.0f;
+  b11 = th * b11 + 0.0f;
+  float b12 = V9I(r129);
+  b12 = th * b12 + V9I(r128);
+  b12 = th * b12 + V9I(r127);
+  b12 = th * b12 + V9I(r126);
+  b12 = th * b12 + V9I(r125);
+  b12 = th * b12 + V9I(r124);
+  b12 = th * b12 + V9I(r123);
+  b12 = th * b12 + V9I(r122);
+  b12 = th * b12 + 0.0f;
+  b12 = th * b12 + 0.0f;
+  float b13 = V9I(r139);
+  b13 = th * b13 + V9I(r138);
+  b13 = th * b13 + V9I(r137);
+  b13 = th * b13 + V9I(r136);
+  b13 = th * b13 + V9I(r135);
+  b13 = th * b13 + V9I(r134);
+  b13 = th * b13 + V9I(r133);
+  b13 = th * b13 + V9I(r132);
+  b13 = th * b13 + 0.0f;
+  b13 = th * b13 + 0.0f;
+  float b14 = V9I(r149);
+  b14 = th * b14 + V9I(r148);
+  b14 = th * b14 + V9I(r147);
+  b14 = th * b14 + V9I(r146);
+  b14 = th * b14 + V9I(r145);
+  b14 = th * b14 + V9I(r144);
+  b14 = th * b14 + V9I(r143);
+  b14 = th * b14 + V9I(r142);
+  b14 = th * b14 + 0.0f;
+  b14 = th * b14 + 0.0f;
+  float b15 = V9I(r159);
+  b15 = th * b15 + V9I(r158);
+  b15 = th * b15 + V9I(r157);
+  b15 = th * b15 + V9I(r156);
+  b15 = th * b15 + V9I(r155);
+  b15 = th * b15 + V9I(r154);
+  b15 = th * b15 + V9I(r153);
+  b15 = th * b15 + V9I(r152);
+  b15 = th * b15 + 0.0f;
+  b15 = th * b15 + 0.0f;
+  float b17 = V9I(r179);
+  b17 = th * b17 + V9I(r178);
+  b17 = th * b17 + V9I(r177);
+  b17 = th * b17 + V9I(r176);
+  b17 = th * b17 + V9I(r175);
+  b17 = th * b17 + V9I(r174);
+  b17 = th * b17 + V9I(r173);
+  b17 = th * b17 + V9I(r172);
+  b17 = th * b17 + 0.0f;
+  b17 = th * b17 + 0.0f;
+  float b18 = V9I(r189);
+  b18 = th * b18 + V9I(r188);
+  b18 = th * b18 + V9I(r187);
+  b18 = th * b18 + V9I(r186);
+  b18 = th * b18 + V9I(r185);
+  b18 = th * b18 + V9I(r184);
+  b18 = th * b18 + V9I(r183);
+  b18 = th * b18 + V9I(r182);
+  b18 = th * b18 + 0.0f;
+  b18 = th * b18 + 0.0f;
+  float b19 = V9I(r199);
+  b19 = th * b19 + V9I(r198);
+  b19 = th * b19 + V9I(r197);
+  b19 = th * b19 + V9I(r196);
+  b19 = th * b19 + V9I(r195);
+  b19 = th * b19 + V9I(r194);
+  b19 = th * b19 + V9I(r193);
+  b19 = th * b19 + V9I(r192);
+  b19 = th * b19 + 0.0f;
+  b19 = th * b19 + 0.0f;
+  float b20 = V9I(r209);
+  b20 = th * b20 + V9I(r208);
+  b20 = th * b20 + V9I(r207);
+  b20 = th * b20 + V9I(r206);
+  b20 = th * b20 + V9I(r205);
+  b20 = th * b20 + V9I(r204);
+  b20 = th * b20 + V9I(r203);
+  b20 = th * b20 + V9I(r202);
+  b20 = th * b20 + 0.0f;
+  b20 = th * b20 + 0.0f;
+  float b21 = V9I(r219);
+  b21 = th * b21 + V9I(r218);
+  b21 = th * b21 + V9I(r217);
+  b21 = th * b21 + V9I(r216);
+  b21 = th * b21 + V9I(r215);
+  b21 = th * b21 + V9I(r214);
+  b21 = th * b21 + V9I(r213);
+  b21 = th * b21 + V9I(r212);
+  b21 = th * b21 + 0.0f;
+  b21 = th * b21 + 0.0f;
+  float b22 = V9I(r229);
+  b22 = th * b22 + V9I(r228);
+  b22 = th * b22 + V9I(r227);
+  b22 = th * b22 + V9I(r226);
+  b22 = th * b22 + V9I(r225);
+  b22 = th * b22 + V9I(r224);
+  b22 = th * b22 + V9I(r223);
+  b22 = th * b22 + V9I(r222);
+  b22 = th * b22 + 0.0f;
+  b22 = th * b22 + 0.0f;
+  float b23 = V9I(r239);
+  b23 = th * b23 + V9I(r238);
+  b23 = th * b23 + V9I(r237);
+  b23 = th * b23 + V9I(r236);
+  b23 = th * b23 + V9I(r235);
+  b23 = th * b23 + V9I(r234);
+  b23 = th * b23 + V9I(r233);
+  b23 = th * b23 + V9I(r232);
+  b23 = th * b23 + 0.0f;
+  b23 = th * b23 + 0.0f;
+  float b24 = V9I(r249);
+  b24 = th * b24 + V9I(r248);
+  b24 = th * b24 + V9I(r247);
+  b24 = th * b24 + V9I(r246);
+  b24 = th * b24 + V9I(r245);
+  b24 = th * b24 + V9I(r244);
+  b24 = th * b24 + V9I(r243);
+  b24 = th * b24 + V9I(r242);
+  b24 = th * b24 + 0.0f;
+  b24 = th * b24 + 0.0f;
+  float b25 = V9I(r259);
+  b25 = th * b25 + V9I(r258);
+  b25 = th * b25 + V9I(r257);
+  b25 = th * b25 + V9I(r256);
+  b25 = th * b25 + V9I(r255);
+  b25 = th * b25 + V9I(r254);
+  b25 = th * b25 + V9I(r253);
+  b25 = th * b25 + V9I(r252);
+  b25 = th * b25 + 0.0f;
+  b25 = th * b25 + 0.0f;
+  float b26 = V9I(r269);
+  b26 = th * b26 + V9I(r268);
+  b26 = th * b26 + V9I(r267);
+  b26 = th * b26 + V9I(r266);
+  b26 = th * b26 + V9I(r265);
+  b26 = th * b26 + V9I(r264);
+  b26 = th * b26 + V9I(r263);
+  b26 = th * b26 + V9I(r262);
+  b26 = th * b26 + 0.0f;
+  b26 = th * b26 + 0.0f;
+#pragma unroll
+  for (int i = 0; i < N; i++) out[i] = up[i] + dt * (k[0][i] * b1 + k[1][i] * b8 + k[2][i] * b9 + k[3][i] * b10 + k[4][i] * b11 + k[5][i] * b12 + k[6][i] * b13 + k[7][i] * b14 + k[8][i] * b15 + e17[i] * b17 + e18[i] * b18 + e19[i] * b19 + e20[i] * b20 + e21[i] * b21 + e22[i] * b22 + e23[i] * b23 + e24[i] * b24 + e25[i] * b25 + e26[i] * b26);
+}
+#endif
+
+#if DEGPU_ALG <= 3 || DEGPU_ALG == 5 || DEGPU_ALG == 6
 // ------------------------------------------------------------------ driver pieces (kernels.jl)
 // Loop-invariant kernel parameters copied into registers once per thread (reading them
 // through a reference to the parameter block inside the step loop costs a constant-bank
@@ -1301,7 +1607,7 @@ DEGPU_DEV void lane_finish(Lane& L, const Io& io, int i) {
   if (io.P.naccept) io.P.naccept[i] = L.naccept;
   if (io.P.nreject) io.P.nreject[i] = L.nreject;
 }
-#endif  // DEGPU_ALG <= 3 || DEGPU_ALG == 5
+#endif  // DEGPU_ALG <= 3 || DEGPU_ALG == 5 || DEGPU_ALG == 6
 
 }  // namespace degpu
 

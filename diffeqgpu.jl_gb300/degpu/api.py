@@ -62,6 +62,10 @@ class GPUVern7(GPUODEAlgorithm):
     alg_id, order = _lib.ALG_VERN7, 7
 
 
+class GPUVern9(GPUODEAlgorithm):
+    alg_id, order = _lib.ALG_VERN9, 9
+
+
 class GPURosenbrock23(GPUODEImplicitAlgorithm):
     alg_id, order = _lib.ALG_ROSENBROCK23, 2
 

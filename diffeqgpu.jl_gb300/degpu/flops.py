@@ -14,6 +14,7 @@ RHS_FLOPS = {"lorenz": 8, "robertson": 13, "decay": 2, "growth": 0, "osc": 3, "l
 # the error estimate; number of RHS evaluations per attempt (first-same-as-last for Tsit5)
 _TSIT5 = dict(stages=[1, 2, 3, 4, 5], update=6, err=7, rhs=6, stage_times=5)
 _VERN7 = dict(stages=[1, 2, 2, 3, 4, 5, 6, 7, 6], update=7, err=8, rhs=10, stage_times=9)
+_VERN9 = dict(stages=[1, 2, 2, 3, 3, 4, 3, 4, 5, 6, 7, 8, 9, 10, 9], update=9, err=10, rhs=16, stage_times=15)
 
 
 def _explicit(spec, N, rhs, adaptive):
@@ -34,6 +35,8 @@ def attempt_flops(alg: str, N: int, model: str, adaptive: bool = True) -> int:
         return _explicit(_TSIT5, N, rhs, adaptive)
     if alg == "vern7":
         return _explicit(_VERN7, N, rhs, adaptive) - rhs  # k1 once per step, counted in step_flops
+    if alg == "vern9":
+        return _explicit(_VERN9, N, rhs, adaptive) - rhs
     if alg == "rosenbrock23":
         lu = 2 * N ** 3 // 3 + N * N          # factor W
         solve = 2 * N * N                      # one triangular pair
@@ -52,7 +55,7 @@ def attempt_flops(alg: str, N: int, model: str, adaptive: bool = True) -> int:
 def step_flops(alg: str, N: int, model: str) -> int:
     """Per accepted step, work done once per step (not per attempt)."""
     rhs = RHS_FLOPS[model]
-    if alg == "vern7":
+    if alg in ("vern7", "vern9"):
         return rhs
     if alg in ("rosenbrock23", "rodas5p", "rodas4"):
         return 3 * rhs * N  # Jacobian by forward-mode AD ~ N dual sweeps
@@ -65,6 +68,8 @@ def interp_flops(alg: str, N: int, model: str) -> int:
         return 4 * 7 + (2 * 7 + 1) * N + 2
     if alg == "vern7":
         return 13 * 12 + 6 * rhs + (2 * 9 + 1) * 6 * N + 30 * N
+    if alg == "vern9":
+        return 19 * 10 + 10 * rhs + (2 * 11) * 10 * N + (2 * 19 + 1) * N
     if alg == "rosenbrock23":
         return 8 + 5 * N
     if alg == "rodas4":

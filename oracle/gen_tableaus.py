@@ -33,6 +33,8 @@ TABLES = [
     ("vern7x", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern7ExtraStages"),
     ("vern7i", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern7InterpolationCoefficients"),
     ("vern9", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern9Tableau"),
+    ("vern9x", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern9ExtraStages"),
+    ("vern9i", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern9InterpolationCoefficients"),
     ("rodas5p", "src/ensemblegpukernel/tableaus/rodas_tableaus.jl", "Rodas5PTableau"),
     ("rodas4", "src/ensemblegpukernel/tableaus/rodas_tableaus.jl", "Rodas4Tableau"),
 ]
@@ -83,7 +85,7 @@ def main():
     ]
     dev_lines = [
         "// Generated by oracle/gen_tableaus.py -- do not edit.",
-        "// Method coefficients (Verner 7(6), Rodas5P, Rodas4) rounded once from their published FP64",
+        "// Method coefficients (Verner 7(6) and 9(8), Rodas5P, Rodas4) rounded once from their published FP64",
         "// values to FP32, exactly as Julia's convert(Float32, ::Float64) does in the reference",
         "// (see per-table citations).  They live in constant memory and are read as",
         "// constant-bank operands by the stage arithmetic.",
@@ -105,8 +107,6 @@ def main():
             oracle_lines.append(f"  {v!r}, /* {n} */")
         oracle_lines.append("};")
         oracle_lines.append("")
-        if tab == "vern9":
-            continue  # FP64 oracle method only
         dev_lines.append(f"// {cite}")
         dev_lines.append("enum {")
         for n in names:

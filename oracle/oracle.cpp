@@ -52,7 +52,7 @@
 #include "tableaus_gen.h"
 
 /* ------------------------------------------------------------------ constants */
-enum { ALG_TSIT5 = 0, ALG_VERN7 = 1, ALG_RB23 = 2, ALG_RODAS5P = 3, ALG_EM = 4, ALG_RODAS4 = 5 };
+enum { ALG_TSIT5 = 0, ALG_VERN7 = 1, ALG_RB23 = 2, ALG_RODAS5P = 3, ALG_EM = 4, ALG_RODAS4 = 5, ALG_VERN9 = 6 };
 enum { RET_DEFAULT = 0, RET_SUCCESS = 1, RET_TERMINATED = 2, RET_DTMIN = 3, RET_MAXITERS = 4, RET_UNSTABLE = 5 };
 enum { JAC_AD = 0, JAC_ANALYTIC = 1, JAC_FINITEDIFF = 2 };
 enum {
@@ -312,6 +312,7 @@ static Tsit5Tab make_tsit5() {
 static const Tsit5Tab TS5 = make_tsit5();
 
 static float V7[OR_VERN7_COUNT], V7X[OR_VERN7X_COUNT], V7I[OR_VERN7I_COUNT], R5P[OR_RODAS5P_COUNT], R4T[OR_RODAS4_COUNT];
+static float F9[OR_VERN9_COUNT], F9X[OR_VERN9X_COUNT], F9I[OR_VERN9I_COUNT];
 static int tabs_ready = 0;
 static void init_tabs() {
   if (tabs_ready) return;
@@ -323,6 +324,9 @@ static void init_tabs() {
       for (int i = 0; i < OR_VERN7I_COUNT; i++) V7I[i] = (float)OR_VERN7I[i];
       for (int i = 0; i < OR_RODAS5P_COUNT; i++) R5P[i] = (float)OR_RODAS5P[i];
       for (int i = 0; i < OR_RODAS4_COUNT; i++) R4T[i] = (float)OR_RODAS4[i];
+      for (int i = 0; i < OR_VERN9_COUNT; i++) F9[i] = (float)OR_VERN9[i];
+      for (int i = 0; i < OR_VERN9X_COUNT; i++) F9X[i] = (float)OR_VERN9X[i];
+      for (int i = 0; i < OR_VERN9I_COUNT; i++) F9I[i] = (float)OR_VERN9I[i];
       tabs_ready = 1;
     }
   }
@@ -332,6 +336,9 @@ static void init_tabs() {
 #define V7IC(n) V7I[OR_VERN7I_##n]
 #define RPC(n) R5P[OR_RODAS5P_##n]
 #define R4C(n) R4T[OR_RODAS4_##n]
+#define F9C(n) F9[OR_VERN9_##n]
+#define F9XC(n) F9X[OR_VERN9X_##n]
+#define F9IC(n) F9I[OR_VERN9I_##n]
 
 /* ------------------------------------------------------------------ configuration */
 extern "C" {
@@ -568,7 +575,7 @@ static Ctrl make_ctrl(int order) {
   return c;
 }
 static int alg_order(int alg) {
-  return alg == ALG_TSIT5 ? 5 : alg == ALG_VERN7 ? 7 : alg == ALG_RB23 ? 2 : alg == ALG_RODAS5P ? 5 : alg == ALG_RODAS4 ? 4 : 1;
+  return alg == ALG_TSIT5 ? 5 : alg == ALG_VERN7 ? 7 : alg == ALG_RB23 ? 2 : alg == ALG_RODAS5P ? 5 : alg == ALG_RODAS4 ? 4 : alg == ALG_VERN9 ? 9 : 1;
 }
 
 /* PI controller decision, shared by every adaptive step! (e.g. gpu_tsit5_perform_step.jl:124-170).
@@ -599,6 +606,273 @@ static inline float scaled_norm(const float* e, const float* up, const float* u,
   float tmp[MAXN];
   for (int i = 0; i < N; i++) tmp[i] = e[i] / (abstol + jl_max(fabsf(up[i]), fabsf(u[i])) * reltol);
   return ode_norm(tmp, N);
+}
+
+/* ------------------------------------------------------------------ Vern9
+ * gpu_vern9_perform_step.jl:1-319 (16 stages, k1 recomputed every attempt; the dense output
+ * keeps k1, k8..k16) and nonstiff/interpolants.jl:192-371 (10 extra stages, bΘs by
+ * Horner as Julia's evalpoly, evaluated without FMA). */
+template <class Tt>
+static void vern9_stages(int m, Integ<Tt>& ig, const float* p, Tt t, float dt, float* u, float (*k)[MAXN]) {
+  int N = ig.N;
+  float tmp[MAXN], k2[MAXN], k3[MAXN], k4[MAXN], k5[MAXN], k6[MAXN], k7[MAXN];
+  const float* up = ig.uprev;
+  model_f<float>(m, k[0], up, p, t_f32(t));
+  float a = dt * F9C(a0201);
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + a * k[0][i];
+  model_f<float>(m, k2, tmp, p, tstage(t, F9C(c1), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a0301) * k[0][i] + F9C(a0302) * k2[i]);
+  model_f<float>(m, k3, tmp, p, tstage(t, F9C(c2), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a0401) * k[0][i] + F9C(a0403) * k3[i]);
+  model_f<float>(m, k4, tmp, p, tstage(t, F9C(c3), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a0501) * k[0][i] + F9C(a0503) * k3[i] + F9C(a0504) * k4[i]);
+  model_f<float>(m, k5, tmp, p, tstage(t, F9C(c4), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a0601) * k[0][i] + F9C(a0604) * k4[i] + F9C(a0605) * k5[i]);
+  model_f<float>(m, k6, tmp, p, tstage(t, F9C(c5), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a0701) * k[0][i] + F9C(a0704) * k4[i] + F9C(a0705) * k5[i] + F9C(a0706) * k6[i]);
+  model_f<float>(m, k7, tmp, p, tstage(t, F9C(c6), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a0801) * k[0][i] + F9C(a0806) * k6[i] + F9C(a0807) * k7[i]);
+  model_f<float>(m, k[1], tmp, p, tstage(t, F9C(c7), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a0901) * k[0][i] + F9C(a0906) * k6[i] + F9C(a0907) * k7[i] + F9C(a0908) * k[1][i]);
+  model_f<float>(m, k[2], tmp, p, tstage(t, F9C(c8), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a1001) * k[0][i] + F9C(a1006) * k6[i] + F9C(a1007) * k7[i] + F9C(a1008) * k[1][i] + F9C(a1009) * k[2][i]);
+  model_f<float>(m, k[3], tmp, p, tstage(t, F9C(c9), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a1101) * k[0][i] + F9C(a1106) * k6[i] + F9C(a1107) * k7[i] + F9C(a1108) * k[1][i] + F9C(a1109) * k[2][i] + F9C(a1110) * k[3][i]);
+  model_f<float>(m, k[4], tmp, p, tstage(t, F9C(c10), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a1201) * k[0][i] + F9C(a1206) * k6[i] + F9C(a1207) * k7[i] + F9C(a1208) * k[1][i] + F9C(a1209) * k[2][i] + F9C(a1210) * k[3][i] + F9C(a1211) * k[4][i]);
+  model_f<float>(m, k[5], tmp, p, tstage(t, F9C(c11), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a1301) * k[0][i] + F9C(a1306) * k6[i] + F9C(a1307) * k7[i] + F9C(a1308) * k[1][i] + F9C(a1309) * k[2][i] + F9C(a1310) * k[3][i] + F9C(a1311) * k[4][i] + F9C(a1312) * k[5][i]);
+  model_f<float>(m, k[6], tmp, p, tstage(t, F9C(c12), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9C(a1401) * k[0][i] + F9C(a1406) * k6[i] + F9C(a1407) * k7[i] + F9C(a1408) * k[1][i] + F9C(a1409) * k[2][i] + F9C(a1410) * k[3][i] + F9C(a1411) * k[4][i] + F9C(a1412) * k[5][i] + F9C(a1413) * k[6][i]);
+  model_f<float>(m, k[7], tmp, p, tstage(t, F9C(c13), dt));
+  float g16[MAXN];
+  for (int i = 0; i < N; i++) {
+    tmp[i] = up[i] + dt * (F9C(a1501) * k[0][i] + F9C(a1506) * k6[i] + F9C(a1507) * k7[i] + F9C(a1508) * k[1][i] + F9C(a1509) * k[2][i] + F9C(a1510) * k[3][i] + F9C(a1511) * k[4][i] + F9C(a1512) * k[5][i] + F9C(a1513) * k[6][i] + F9C(a1514) * k[7][i]);
+    g16[i] = up[i] + dt * (F9C(a1601) * k[0][i] + F9C(a1606) * k6[i] + F9C(a1607) * k7[i] + F9C(a1608) * k[1][i] + F9C(a1609) * k[2][i] + F9C(a1610) * k[3][i] + F9C(a1611) * k[4][i] + F9C(a1612) * k[5][i] + F9C(a1613) * k[6][i]);
+  }
+  model_f<float>(m, k[8], tmp, p, tstage(t, 1.0f, dt));
+  model_f<float>(m, k[9], g16, p, tstage(t, 1.0f, dt));
+  for (int i = 0; i < N; i++) u[i] = up[i] + dt * (F9C(b1) * k[0][i] + F9C(b8) * k[1][i] + F9C(b9) * k[2][i] + F9C(b10) * k[3][i] + F9C(b11) * k[4][i] + F9C(b12) * k[5][i] + F9C(b13) * k[6][i] + F9C(b14) * k[7][i] + F9C(b15) * k[8][i]);
+}
+// Julia's @evalpoly (Horner from the highest coefficient; no FMA in parity mode)
+template <class Tt>
+static void vern9_interp(int m, const Integ<Tt>& ig, const float* p, float th, float dt, float* out) {
+  int N = ig.N;
+  const float* up = ig.uprev;
+  const float(*k)[MAXN] = ig.k;
+  const Tt tp = ig.tprev;
+  float tmp[MAXN], e17[MAXN], e18[MAXN], e19[MAXN], e20[MAXN], e21[MAXN], e22[MAXN], e23[MAXN], e24[MAXN], e25[MAXN], e26[MAXN];
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a1701) * k[0][i] + F9XC(a1708) * k[1][i] + F9XC(a1709) * k[2][i] + F9XC(a1710) * k[3][i] + F9XC(a1711) * k[4][i] + F9XC(a1712) * k[5][i] + F9XC(a1713) * k[6][i] + F9XC(a1714) * k[7][i] + F9XC(a1715) * k[8][i]);
+  model_f<float>(m, e17, tmp, p, tstage(tp, F9XC(c17), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a1801) * k[0][i] + F9XC(a1808) * k[1][i] + F9XC(a1809) * k[2][i] + F9XC(a1810) * k[3][i] + F9XC(a1811) * k[4][i] + F9XC(a1812) * k[5][i] + F9XC(a1813) * k[6][i] + F9XC(a1814) * k[7][i] + F9XC(a1815) * k[8][i] + F9XC(a1817) * e17[i]);
+  model_f<float>(m, e18, tmp, p, tstage(tp, F9XC(c18), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a1901) * k[0][i] + F9XC(a1908) * k[1][i] + F9XC(a1909) * k[2][i] + F9XC(a1910) * k[3][i] + F9XC(a1911) * k[4][i] + F9XC(a1912) * k[5][i] + F9XC(a1913) * k[6][i] + F9XC(a1914) * k[7][i] + F9XC(a1915) * k[8][i] + F9XC(a1917) * e17[i] + F9XC(a1918) * e18[i]);
+  model_f<float>(m, e19, tmp, p, tstage(tp, F9XC(c19), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a2001) * k[0][i] + F9XC(a2008) * k[1][i] + F9XC(a2009) * k[2][i] + F9XC(a2010) * k[3][i] + F9XC(a2011) * k[4][i] + F9XC(a2012) * k[5][i] + F9XC(a2013) * k[6][i] + F9XC(a2014) * k[7][i] + F9XC(a2015) * k[8][i] + F9XC(a2017) * e17[i] + F9XC(a2018) * e18[i] + F9XC(a2019) * e19[i]);
+  model_f<float>(m, e20, tmp, p, tstage(tp, F9XC(c20), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a2101) * k[0][i] + F9XC(a2108) * k[1][i] + F9XC(a2109) * k[2][i] + F9XC(a2110) * k[3][i] + F9XC(a2111) * k[4][i] + F9XC(a2112) * k[5][i] + F9XC(a2113) * k[6][i] + F9XC(a2114) * k[7][i] + F9XC(a2115) * k[8][i] + F9XC(a2117) * e17[i] + F9XC(a2118) * e18[i] + F9XC(a2119) * e19[i] + F9XC(a2120) * e20[i]);
+  model_f<float>(m, e21, tmp, p, tstage(tp, F9XC(c21), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a2201) * k[0][i] + F9XC(a2208) * k[1][i] + F9XC(a2209) * k[2][i] + F9XC(a2210) * k[3][i] + F9XC(a2211) * k[4][i] + F9XC(a2212) * k[5][i] + F9XC(a2213) * k[6][i] + F9XC(a2214) * k[7][i] + F9XC(a2215) * k[8][i] + F9XC(a2217) * e17[i] + F9XC(a2218) * e18[i] + F9XC(a2219) * e19[i] + F9XC(a2220) * e20[i] + F9XC(a2221) * e21[i]);
+  model_f<float>(m, e22, tmp, p, tstage(tp, F9XC(c22), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a2301) * k[0][i] + F9XC(a2308) * k[1][i] + F9XC(a2309) * k[2][i] + F9XC(a2310) * k[3][i] + F9XC(a2311) * k[4][i] + F9XC(a2312) * k[5][i] + F9XC(a2313) * k[6][i] + F9XC(a2314) * k[7][i] + F9XC(a2315) * k[8][i] + F9XC(a2317) * e17[i] + F9XC(a2318) * e18[i] + F9XC(a2319) * e19[i] + F9XC(a2320) * e20[i] + F9XC(a2321) * e21[i]);
+  model_f<float>(m, e23, tmp, p, tstage(tp, F9XC(c23), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a2401) * k[0][i] + F9XC(a2408) * k[1][i] + F9XC(a2409) * k[2][i] + F9XC(a2410) * k[3][i] + F9XC(a2411) * k[4][i] + F9XC(a2412) * k[5][i] + F9XC(a2413) * k[6][i] + F9XC(a2414) * k[7][i] + F9XC(a2415) * k[8][i] + F9XC(a2417) * e17[i] + F9XC(a2418) * e18[i] + F9XC(a2419) * e19[i] + F9XC(a2420) * e20[i] + F9XC(a2421) * e21[i]);
+  model_f<float>(m, e24, tmp, p, tstage(tp, F9XC(c24), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a2501) * k[0][i] + F9XC(a2508) * k[1][i] + F9XC(a2509) * k[2][i] + F9XC(a2510) * k[3][i] + F9XC(a2511) * k[4][i] + F9XC(a2512) * k[5][i] + F9XC(a2513) * k[6][i] + F9XC(a2514) * k[7][i] + F9XC(a2515) * k[8][i] + F9XC(a2517) * e17[i] + F9XC(a2518) * e18[i] + F9XC(a2519) * e19[i] + F9XC(a2520) * e20[i] + F9XC(a2521) * e21[i]);
+  model_f<float>(m, e25, tmp, p, tstage(tp, F9XC(c25), dt));
+  for (int i = 0; i < N; i++) tmp[i] = up[i] + dt * (F9XC(a2601) * k[0][i] + F9XC(a2608) * k[1][i] + F9XC(a2609) * k[2][i] + F9XC(a2610) * k[3][i] + F9XC(a2611) * k[4][i] + F9XC(a2612) * k[5][i] + F9XC(a2613) * k[6][i] + F9XC(a2614) * k[7][i] + F9XC(a2615) * k[8][i] + F9XC(a2617) * e17[i] + F9XC(a2618) * e18[i] + F9XC(a2619) * e19[i] + F9XC(a2620) * e20[i] + F9XC(a2621) * e21[i]);
+  model_f<float>(m, e26, tmp, p, tstage(tp, F9XC(c26), dt));
+  float b1 = F9IC(r019);
+  b1 = th * b1 + F9IC(r018);
+  b1 = th * b1 + F9IC(r017);
+  b1 = th * b1 + F9IC(r016);
+  b1 = th * b1 + F9IC(r015);
+  b1 = th * b1 + F9IC(r014);
+  b1 = th * b1 + F9IC(r013);
+  b1 = th * b1 + F9IC(r012);
+  b1 = th * b1 + F9IC(r011);
+  b1 = th * b1 + 0.0f;
+  float b8 = F9IC(r089);
+  b8 = th * b8 + F9IC(r088);
+  b8 = th * b8 + F9IC(r087);
+  b8 = th * b8 + F9IC(r086);
+  b8 = th * b8 + F9IC(r085);
+  b8 = th * b8 + F9IC(r084);
+  b8 = th * b8 + F9IC(r083);
+  b8 = th * b8 + F9IC(r082);
+  b8 = th * b8 + 0.0f;
+  b8 = th * b8 + 0.0f;
+  float b9 = F9IC(r099);
+  b9 = th * b9 + F9IC(r098);
+  b9 = th * b9 + F9IC(r097);
+  b9 = th * b9 + F9IC(r096);
+  b9 = th * b9 + F9IC(r095);
+  b9 = th * b9 + F9IC(r094);
+  b9 = th * b9 + F9IC(r093);
+  b9 = th * b9 + F9IC(r092);
+  b9 = th * b9 + 0.0f;
+  b9 = th * b9 + 0.0f;
+  float b10 = F9IC(r109);
+  b10 = th * b10 + F9IC(r108);
+  b10 = th * b10 + F9IC(r107);
+  b10 = th * b10 + F9IC(r106);
+  b10 = th * b10 + F9IC(r105);
+  b10 = th * b10 + F9IC(r104);
+  b10 = th * b10 + F9IC(r103);
+  b10 = th * b10 + F9IC(r102);
+  b10 = th * b10 + 0.0f;
+  b10 = th * b10 + 0.0f;
+  float b11 = F9IC(r119);
+  b11 = th * b11 + F9IC(r118);
+  b11 = th * b11 + F9IC(r117);
+  b11 = th * b11 + F9IC(r116);
+  b11 = th * b11 + F9IC(r115);
+  b11 = th * b11 + F9IC(r114);
+  b11 = th * b11 + F9IC(r113);
+  b11 = th * b11 + F9IC(r112);
+  b11 = th * b11 + 0.0f;
+  b11 = th * b11 + 0.0f;
+  float b12 = F9IC(r129);
+  b12 = th * b12 + F9IC(r128);
+  b12 = th * b12 + F9IC(r127);
+  b12 = th * b12 + F9IC(r126);
+  b12 = th * b12 + F9IC(r125);
+  b12 = th * b12 + F9IC(r124);
+  b12 = th * b12 + F9IC(r123);
+  b12 = th * b12 + F9IC(r122);
+  b12 = th * b12 + 0.0f;
+  b12 = th * b12 + 0.0f;
+  float b13 = F9IC(r139);
+  b13 = th * b13 + F9IC(r138);
+  b13 = th * b13 + F9IC(r137);
+  b13 = th * b13 + F9IC(r136);
+  b13 = th * b13 + F9IC(r135);
+  b13 = th * b13 + F9IC(r134);
+  b13 = th * b13 + F9IC(r133);
+  b13 = th * b13 + F9IC(r132);
+  b13 = th * b13 + 0.0f;
+  b13 = th * b13 + 0.0f;
+  float b14 = F9IC(r149);
+  b14 = th * b14 + F9IC(r148);
+  b14 = th * b14 + F9IC(r147);
+  b14 = th * b14 + F9IC(r146);
+  b14 = th * b14 + F9IC(r145);
+  b14 = th * b14 + F9IC(r144);
+  b14 = th * b14 + F9IC(r143);
+  b14 = th * b14 + F9IC(r142);
+  b14 = th * b14 + 0.0f;
+  b14 = th * b14 + 0.0f;
+  float b15 = F9IC(r159);
+  b15 = th * b15 + F9IC(r158);
+  b15 = th * b15 + F9IC(r157);
+  b15 = th * b15 + F9IC(r156);
+  b15 = th * b15 + F9IC(r155);
+  b15 = th * b15 + F9IC(r154);
+  b15 = th * b15 + F9IC(r153);
+  b15 = th * b15 + F9IC(r152);
+  b15 = th * b15 + 0.0f;
+  b15 = th * b15 + 0.0f;
+  float b17 = F9IC(r179);
+  b17 = th * b17 + F9IC(r178);
+  b17 = th * b17 + F9IC(r177);
+  b17 = th * b17 + F9IC(r176);
+  b17 = th * b17 + F9IC(r175);
+  b17 = th * b17 + F9IC(r174);
+  b17 = th * b17 + F9IC(r173);
+  b17 = th * b17 + F9IC(r172);
+  b17 = th * b17 + 0.0f;
+  b17 = th * b17 + 0.0f;
+  float b18 = F9IC(r189);
+  b18 = th * b18 + F9IC(r188);
+  b18 = th * b18 + F9IC(r187);
+  b18 = th * b18 + F9IC(r186);
+  b18 = th * b18 + F9IC(r185);
+  b18 = th * b18 + F9IC(r184);
+  b18 = th * b18 + F9IC(r183);
+  b18 = th * b18 + F9IC(r182);
+  b18 = th * b18 + 0.0f;
+  b18 = th * b18 + 0.0f;
+  float b19 = F9IC(r199);
+  b19 = th * b19 + F9IC(r198);
+  b19 = th * b19 + F9IC(r197);
+  b19 = th * b19 + F9IC(r196);
+  b19 = th * b19 + F9IC(r195);
+  b19 = th * b19 + F9IC(r194);
+  b19 = th * b19 + F9IC(r193);
+  b19 = th * b19 + F9IC(r192);
+  b19 = th * b19 + 0.0f;
+  b19 = th * b19 + 0.0f;
+  float b20 = F9IC(r209);
+  b20 = th * b20 + F9IC(r208);
+  b20 = th * b20 + F9IC(r207);
+  b20 = th * b20 + F9IC(r206);
+  b20 = th * b20 + F9IC(r205);
+  b20 = th * b20 + F9IC(r204);
+  b20 = th * b20 + F9IC(r203);
+  b20 = th * b20 + F9IC(r202);
+  b20 = th * b20 + 0.0f;
+  b20 = th * b20 + 0.0f;
+  float b21 = F9IC(r219);
+  b21 = th * b21 + F9IC(r218);
+  b21 = th * b21 + F9IC(r217);
+  b21 = th * b21 + F9IC(r216);
+  b21 = th * b21 + F9IC(r215);
+  b21 = th * b21 + F9IC(r214);
+  b21 = th * b21 + F9IC(r213);
+  b21 = th * b21 + F9IC(r212);
+  b21 = th * b21 + 0.0f;
+  b21 = th * b21 + 0.0f;
+  float b22 = F9IC(r229);
+  b22 = th * b22 + F9IC(r228);
+  b22 = th * b22 + F9IC(r227);
+  b22 = th * b22 + F9IC(r226);
+  b22 = th * b22 + F9IC(r225);
+  b22 = th * b22 + F9IC(r224);
+  b22 = th * b22 + F9IC(r223);
+  b22 = th * b22 + F9IC(r222);
+  b22 = th * b22 + 0.0f;
+  b22 = th * b22 + 0.0f;
+  float b23 = F9IC(r239);
+  b23 = th * b23 + F9IC(r238);
+  b23 = th * b23 + F9IC(r237);
+  b23 = th * b23 + F9IC(r236);
+  b23 = th * b23 + F9IC(r235);
+  b23 = th * b23 + F9IC(r234);
+  b23 = th * b23 + F9IC(r233);
+  b23 = th * b23 + F9IC(r232);
+  b23 = th * b23 + 0.0f;
+  b23 = th * b23 + 0.0f;
+  float b24 = F9IC(r249);
+  b24 = th * b24 + F9IC(r248);
+  b24 = th * b24 + F9IC(r247);
+  b24 = th * b24 + F9IC(r246);
+  b24 = th * b24 + F9IC(r245);
+  b24 = th * b24 + F9IC(r244);
+  b24 = th * b24 + F9IC(r243);
+  b24 = th * b24 + F9IC(r242);
+  b24 = th * b24 + 0.0f;
+  b24 = th * b24 + 0.0f;
+  float b25 = F9IC(r259);
+  b25 = th * b25 + F9IC(r258);
+  b25 = th * b25 + F9IC(r257);
+  b25 = th * b25 + F9IC(r256);
+  b25 = th * b25 + F9IC(r255);
+  b25 = th * b25 + F9IC(r254);
+  b25 = th * b25 + F9IC(r253);
+  b25 = th * b25 + F9IC(r252);
+  b25 = th * b25 + 0.0f;
+  b25 = th * b25 + 0.0f;
+  float b26 = F9IC(r269);
+  b26 = th * b26 + F9IC(r268);
+  b26 = th * b26 + F9IC(r267);
+  b26 = th * b26 + F9IC(r266);
+  b26 = th * b26 + F9IC(r265);
+  b26 = th * b26 + F9IC(r264);
+  b26 = th * b26 + F9IC(r263);
+  b26 = th * b26 + F9IC(r262);
+  b26 = th * b26 + 0.0f;
+  b26 = th * b26 + 0.0f;
+  for (int i = 0; i < N; i++) out[i] = up[i] + dt * (k[0][i] * b1 + k[1][i] * b8 + k[2][i] * b9 + k[3][i] * b10 + k[4][i] * b11 + k[5][i] * b12 + k[6][i] * b13 + k[7][i] * b14 + k[8][i] * b15 + e17[i] * b17 + e18[i] * b18 + e19[i] * b19 + e20[i] * b20 + e21[i] * b21 + e22[i] * b22 + e23[i] * b23 + e24[i] * b24 + e25[i] * b25 + e26[i] * b26);
 }
 
 /* ------------------------------------------------------------------ Rosenbrock23 */
@@ -752,6 +1026,7 @@ static void interpolate(int m, int alg, const Integ<Tt>& ig, const float* p, flo
         out[i] = y0[i] + dt * (b[0] * ig.k[0][i] + b[1] * ig.k[1][i] + b[2] * ig.k[2][i] + b[3] * ig.k[3][i] + b[4] * ig.k[4][i] + b[5] * ig.k[5][i] + b[6] * ig.k[6][i]);
     } break;
     case ALG_VERN7: vern7_interp(m, ig, p, th, dt, out); break;
+    case ALG_VERN9: vern9_interp(m, ig, p, th, dt, out); break;
     case ALG_RB23: { /* nonstiff/interpolants.jl:389-399 */
       const float d = 1.0f / (2.0f + sqrtf(2.0f));
       float c1 = th * (1.0f - th) / (1.0f - 2.0f * d);
@@ -1016,6 +1291,8 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
         tsit5_stages(m, ig, p, t, dt, k1, u, ig.k, 1);
       } else if (alg == ALG_VERN7) {
         vern7_stages(m, ig, p, t, dt, u, ig.k);
+      } else if (alg == ALG_VERN9) {
+        vern9_stages(m, ig, p, t, dt, u, ig.k);
       } else if (alg == ALG_RB23) {
         float err[MAXN];
         rb23_attempt(m, cfg->jac, ig, p, t, dt, u, ig.k[0], ig.k[1], err, 0);
@@ -1056,6 +1333,10 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
           vern7_stages(m, ig, p, t, dt, u, kk);
           for (int i = 0; i < N; i++)
             err[i] = dt * (V7C(btilde1) * kk[0][i] + V7C(btilde4) * kk[3][i] + V7C(btilde5) * kk[4][i] + V7C(btilde6) * kk[5][i] + V7C(btilde7) * kk[6][i] + V7C(btilde8) * kk[7][i] + V7C(btilde9) * kk[8][i] + V7C(btilde10) * kk[9][i]);
+        } else if (alg == ALG_VERN9) {
+          vern9_stages(m, ig, p, t, dt, u, kk);
+          for (int i = 0; i < N; i++)
+            err[i] = dt * (F9C(btilde1) * kk[0][i] + F9C(btilde8) * kk[1][i] + F9C(btilde9) * kk[2][i] + F9C(btilde10) * kk[3][i] + F9C(btilde11) * kk[4][i] + F9C(btilde12) * kk[5][i] + F9C(btilde13) * kk[6][i] + F9C(btilde14) * kk[7][i] + F9C(btilde15) * kk[8][i] + F9C(btilde16) * kk[9][i]);
         } else if (alg == ALG_RB23) {
           rb23_attempt(m, cfg->jac, ig, p, t, dt, u, kk[0], kk[1], err, 1);
         } else if (alg == ALG_RODAS4) { /* error estimate is k6 */
@@ -1065,7 +1346,7 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
         }
         EEst = scaled_norm(err, ig.uprev, u, N, ig.abstol, ig.reltol);
         if (controller(ig, C, EEst, dt, t)) {
-          int ns = alg == ALG_TSIT5 ? 7 : alg == ALG_VERN7 ? 10 : (alg == ALG_RB23 || alg == ALG_RODAS4) ? 2 : 3;
+          int ns = alg == ALG_TSIT5 ? 7 : (alg == ALG_VERN7 || alg == ALG_VERN9) ? 10 : (alg == ALG_RB23 || alg == ALG_RODAS4) ? 2 : 3;
           for (int s = 0; s < ns; s++) for (int i = 0; i < N; i++) ig.k[s][i] = kk[s][i];
           for (int i = 0; i < N; i++) ig.u[i] = u[i];
           /* not snapped to tf: stop at the next tstop, u = integ(tstop) (:157-167) */

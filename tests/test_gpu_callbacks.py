@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 EPS32 = float(np.finfo(np.float32).eps)
 ALGS = {"tsit5": "GPUTsit5", "vern7": "GPUVern7", "rosenbrock23": "GPURosenbrock23", "rodas5p": "GPURodas5P",
-        "rodas4": "GPURodas4"}
+        "rodas4": "GPURodas4", "vern9": "GPUVern9"}
 
 
 def run_pair(degpu, oracle, model, alg, u0, p, tspan, tt, *, adaptive, dt, callbacks, tstops=None, saveat=None,
@@ -78,7 +78,7 @@ def ball_exact(h0, g, t):
 
 
 # ----------------------------------------------------------------------------- continuous
-@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "vern9"])
 @pytest.mark.parametrize("adaptive", [False, True])
 @pytest.mark.parametrize("tt", [np.float32, np.float64])
 def test_bouncing_ball_parity(degpu_mod, oracle_mod, alg, adaptive, tt):
@@ -160,7 +160,7 @@ def test_stiff_bouncing_ball_parity(degpu_mod, oracle_mod, alg, adaptive):
 
 
 # ----------------------------------------------------------------------------- discrete
-@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p", "rodas4"])
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p", "rodas4", "vern9"])
 def test_discrete_tstops_parity(degpu_mod, oracle_mod, alg):
     """gpu_ode_discrete_callbacks.jl: condition t == 2.4f0 with tstops [2.4f0], dt 1f0; the
     dt 0.01f0 / tstops [4.0f0] truncation case; CallbackSet at 2.4 and 4.0 with saveat [0, 6]
@@ -189,7 +189,7 @@ def test_discrete_tstops_parity(degpu_mod, oracle_mod, alg):
             t = float(ts[l])
             # a row saved at an event time holds the value before the affect
             exact = 10 * np.exp(-t) + sum(10 * np.exp(-(t - s)) for s in ev if s < t - 1e-5)
-            rt = {"tsit5": 5e-3, "vern7": 5e-3, "rosenbrock23": 0.15, "rodas5p": 2e-2, "rodas4": 2e-2}[alg]  # fixed dt 1 on u' = -u
+            rt = {"tsit5": 5e-3, "vern7": 5e-3, "rosenbrock23": 0.15, "rodas5p": 2e-2, "rodas4": 2e-2, "vern9": 5e-3}[alg]  # fixed dt 1 on u' = -u
             assert abs(us[l] - exact) < rt * max(1.0, exact), (c, l, t, us[l], exact)
 
 

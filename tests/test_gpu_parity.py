@@ -14,7 +14,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 ALGS = {"tsit5": "GPUTsit5", "vern7": "GPUVern7", "rosenbrock23": "GPURosenbrock23", "rodas5p": "GPURodas5P",
-        "rodas4": "GPURodas4"}
+        "rodas4": "GPURodas4", "vern9": "GPUVern9"}
 
 
 def lorenz_batch(B, seed=0, chaotic=True):
@@ -64,7 +64,7 @@ def assert_saved_equal(us, ous, ts, t0):
 
 
 # ----------------------------------------------------------------------------- fixed step
-@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "vern9"])
 @pytest.mark.parametrize("tt", [np.float32, np.float64])
 def test_fixed_step_bit_parity_lorenz(degpu_mod, oracle_mod, alg, tt):
     """Lorenz ensemble, fixed dt=0.1f0, tspan (0,10), final state only: 10,000 trajectories
@@ -91,7 +91,7 @@ def test_fixed_step_save_everystep_parity(degpu_mod, oracle_mod):
     assert_bit_equal(ts, ots, "ts")
 
 
-@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p", "rodas4"])
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p", "rodas4", "vern9"])
 def test_fixed_step_saveat_parity(degpu_mod, oracle_mod, alg):
     u0, p = lorenz_batch(300, seed=3, chaotic=False)
     sa = np.array([0.0, 0.25, 2.0, 4.0, 5.05, 10.0], np.float32)
@@ -114,7 +114,7 @@ def test_fixed_step_fast_mode_close(degpu_mod, oracle_mod):
 
 
 # ----------------------------------------------------------------------------- adaptive
-@pytest.mark.parametrize("alg", ["tsit5", "vern7"])
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "vern9"])
 @pytest.mark.parametrize("driver", ["naive", "persistent"])
 @pytest.mark.parametrize("tt", [np.float32, np.float64])
 def test_adaptive_saveat_bit_parity(degpu_mod, oracle_mod, alg, driver, tt):
