@@ -103,9 +103,11 @@ CHECKS = [  # (alg, driver, time type, parity, model, extra defines) compiled by
     (3, 1, "double", 1, "lorenz", ""), (5, 2, "double", 0, "lorenz", ""), (6, 2, "double", 0, "lorenz", ""),
     # tstops + callbacks: continuous (bouncing ball) and discrete (decay) sets
     (0, 2, "double", 0, "ball", "-DDEGPU_NCCB=2 -DDEGPU_TSTOPS=1"),
+    # SDE driver: Euler-Maruyama and SIEA on geometric Brownian motion
+    (4, 3, "float", 1, "gbm", ""), (7, 3, "double", 0, "gbm", ""),
     (1, 0, "float", 1, "decay", "-DDEGPU_NDCB=2 -DDEGPU_TSTOPS=1"),
 ]
-MODEL_DIMS = {"lorenz": (3, 3), "ball": (2, 1), "decay": (1, 1)}
+MODEL_DIMS = {"lorenz": (3, 3), "ball": (2, 1), "decay": (1, 1), "gbm": (1, 2)}
 
 
 def check_kernels(verbose: bool = False) -> list[str]:

@@ -117,6 +117,8 @@ struct degpu_rhs_s {
 
 namespace {
 
+bool is_sde_alg(int alg) { return alg == DEGPU_ALG_EM || alg == DEGPU_ALG_SIEA; }
+
 struct KernelSpec {
   int alg, driver, tt, parity, jac, tgrad, refine;
   int tstops = 0, nccb = 0, ndcb = 0;  // tstops / callback set compiled into the kernel
@@ -353,7 +355,7 @@ struct Request {
 };
 
 int resolve_driver(const degpu_options* o, int adaptive) {
-  if (o->alg == DEGPU_ALG_EM) return 3;
+  if (is_sde_alg(o->alg)) return 3;
   if (!adaptive) return 0;
   if (o->driver == DEGPU_DRIVER_NAIVE) return 1;
   return 2;
@@ -364,11 +366,12 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   if (!f || !pr || !o || !out) return fail(DEGPU_E_INVALID, "null argument");
   if (pr->B < 0) return fail(DEGPU_E_INVALID, "negative trajectory count");
   if (pr->B > 0x7fffffffLL) return fail(DEGPU_E_INVALID, "more than 2^31-1 trajectories in one call; split into batches");
-  if (o->alg < 0 || o->alg > 6) return fail(DEGPU_E_INVALID, "unknown algorithm");
-  if (o->alg == DEGPU_ALG_EM && adaptive)
-    return fail(DEGPU_E_UNSUPPORTED, "Adaptive time-stepping is not supported yet with GPUEM.");
-  if (o->alg == DEGPU_ALG_EM && !(f->flags & DEGPU_RHS_HAS_NOISE))
-    return fail(DEGPU_E_INVALID, "GPUEM needs a right-hand side with a noise function (DEGPU_RHS_HAS_NOISE)");
+  if (o->alg < 0 || o->alg > 7) return fail(DEGPU_E_INVALID, "unknown algorithm");
+  if (is_sde_alg(o->alg) && adaptive)
+    return fail(DEGPU_E_UNSUPPORTED, o->alg == DEGPU_ALG_EM ? "Adaptive time-stepping is not supported yet with GPUEM."
+                                                            : "Adaptive time-stepping is not supported yet with GPUSIEA.");
+  if (is_sde_alg(o->alg) && !(f->flags & DEGPU_RHS_HAS_NOISE))
+    return fail(DEGPU_E_INVALID, "GPUEM / GPUSIEA need a right-hand side with a noise function (DEGPU_RHS_HAS_NOISE)");
   if (o->time_type != DEGPU_TIME_F32 && o->time_type != DEGPU_TIME_F64) return fail(DEGPU_E_INVALID, "time_type");
   if (o->mode != DEGPU_MODE_FAST && o->mode != DEGPU_MODE_PARITY) return fail(DEGPU_E_INVALID, "mode");
   if (!(o->dt > 0.0) && !o->dt0) return fail(DEGPU_E_INVALID, "dt must be positive");
@@ -430,8 +433,8 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   if (nc < 0 || nd < 0 || nc > DEGPU_MAX_CALLBACKS || nd > DEGPU_MAX_CALLBACKS)
     return fail(DEGPU_E_INVALID, "at most 8 continuous and 8 discrete callbacks per set");
   if ((nc && !cb->continuous) || (nd && !cb->discrete)) return fail(DEGPU_E_INVALID, "callback array missing");
-  if (o->alg == DEGPU_ALG_EM && (nc || nd || o->ntstops))
-    return fail(DEGPU_E_UNSUPPORTED, "GPUEM takes no callbacks or tstops (em_kernel, gpu_em_perform_step.jl)");
+  if (is_sde_alg(o->alg) && (nc || nd || o->ntstops))
+    return fail(DEGPU_E_UNSUPPORTED, "GPUEM / GPUSIEA take no callbacks or tstops (em_kernel, siea_kernel)");
   for (int j = 0; j < nc; j++) {
     const degpu_continuous_callback& c = cb->continuous[j];
     if (c.fn < 0 || c.rootfind < 0 || c.rootfind > 2 || !(c.abstol >= 0.0) || !(c.dtrelax > 0.0))
@@ -601,7 +604,7 @@ const char* degpu_builtin_rhs(const char* name, int* n_state, int* n_param, int*
 
 int degpu_vectorized_solve(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
                            degpu_outputs* out, void* stream) {
-  if (opt && opt->alg == DEGPU_ALG_EM) return fail(DEGPU_E_INVALID, "GPUEM solves SDE problems: use degpu_vectorized_solve_sde");
+  if (opt && is_sde_alg(opt->alg)) return fail(DEGPU_E_INVALID, "GPUEM / GPUSIEA solve SDE problems: use degpu_vectorized_solve_sde");
   return run(f, probs, opt, 0, out, stream);
 }
 
@@ -612,7 +615,7 @@ int degpu_vectorized_asolve(const degpu_rhs* f, const degpu_problems* probs, con
 
 int degpu_vectorized_solve_sde(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
                                degpu_outputs* out, void* stream) {
-  if (opt && opt->alg != DEGPU_ALG_EM) return fail(DEGPU_E_INVALID, "SDE problems are solved with GPUEM");
+  if (opt && !is_sde_alg(opt->alg)) return fail(DEGPU_E_INVALID, "SDE problems are solved with GPUEM or GPUSIEA");
   return run(f, probs, opt, 0, out, stream);
 }
 
@@ -668,7 +671,7 @@ int degpu_batch_solve_host(const degpu_rhs* f, const float* u0, const float* p, 
         if (n_sa) o.saveat = d + o_sa;
         degpu_outputs out{v_ts, (float*)v_us, L, (signed char*)v_rc, (int*)v_na, (int*)v_nr, nullptr};
         unsigned long long* work = reinterpret_cast<unsigned long long*>(d + o_work);
-        rc = (opt->alg == DEGPU_ALG_EM) ? degpu_vectorized_solve_sde(f, &pr, &o, &out, s)
+        rc = is_sde_alg(opt->alg) ? degpu_vectorized_solve_sde(f, &pr, &o, &out, s)
                                         : (adaptive ? degpu_internal_asolve_with_work(f, &pr, &o, &out, work, s)
                                                     : degpu_vectorized_solve(f, &pr, &o, &out, s));
       }
@@ -762,7 +765,7 @@ int degpu_batch_solve_host(const degpu_rhs* f, const float* u0, const float* p, 
                       retcode ? (signed char*)(d + off_rc) + c0 : nullptr, naccept ? (int*)(d + off_na) + c0 : nullptr,
                       nreject ? (int*)(d + off_nr) + c0 : nullptr, nullptr};
     unsigned long long* work = reinterpret_cast<unsigned long long*>(d + off_work + 256 * (size_t)ci);
-    rc = (opt->alg == DEGPU_ALG_EM) ? degpu_vectorized_solve_sde(f, &pr, &o, &out, cs)
+    rc = is_sde_alg(opt->alg) ? degpu_vectorized_solve_sde(f, &pr, &o, &out, cs)
                                     : (adaptive ? degpu_internal_asolve_with_work(f, &pr, &o, &out, work, cs)
                                                 : degpu_vectorized_solve(f, &pr, &o, &out, cs));
     if (rc) break;

@@ -5,7 +5,7 @@
 // defines, per translation unit:
 //   DEGPU_N, DEGPU_P        state / parameter dimensions
 //   DEGPU_TT                time type (float: the reference's Float32 tspan; double: FP64 time)
-//   DEGPU_ALG               0 Tsit5, 1 Vern7, 2 Rosenbrock23, 3 Rodas5P, 4 EM, 5 Rodas4, 6 Vern9
+//   DEGPU_ALG               0 Tsit5, 1 Vern7, 2 Rosenbrock23, 3 Rodas5P, 4 EM, 5 Rodas4, 6 Vern9, 7 SIEA
 //   DEGPU_DRIVER            0 fixed step, 1 adaptive (one trajectory per thread),
 //                           2 adaptive persistent (warp refill + work stealing), 3 EM
 //   DEGPU_PARITY            1: no FMA (set by --fmad=false), portable pow, Cramer solves
@@ -1694,7 +1694,9 @@ extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCK
 #endif
 
 #if DEGPU_DRIVER == 3
-// em_kernel (perform_step/gpu_em_perform_step.jl:1-74).  The reference seeds Julia's
+// em_kernel (perform_step/gpu_em_perform_step.jl:1-74) and, with DEGPU_ALG 7, siea_kernel
+// (perform_step/gpu_siea_perform_step.jl:48-139): same driver, one normal per component and
+// step.  The reference seeds Julia's
 // device RNG with prob.seed; here each trajectory draws from a counter-based
 // Philox4x32-10 stream (Salmon et al., SC'11) keyed by `seed`, counter
 // (step, trajectory, block), with Box-Muller normals.
@@ -1774,8 +1776,39 @@ extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCK
     degpu_g<float>(g, up, p, TP::f32(t));
 #pragma unroll
     for (int b = 0; b < (N + 3) / 4; b++) normals4(P.seed, (uint32_t)(j - 2), gi, (uint32_t)b, z + 4 * b);
+#if DEGPU_ALG == 7
+    // siea_kernel (perform_step/gpu_siea_perform_step.jl:48-139), diagonal noise, with the
+    // SIEAConstantCache coefficients (:23-47) written out: α1 = α2 = γ1 = 1/2, λ0 = λbar0 =
+    // ν1 = β2 = µ0 = µbar0 = 1, δ2 = -1, ν2 = β3 = δ3 = 0, λ1 = λ3 = µ1 = µ2 = 1/4, λ2 = µ3 = -1/4
+    {
+      float dW[N], W2[N], W3[N], x[N], k1[N], g1[N], g2[N];
+#pragma unroll
+      for (int c = 0; c < N; c++) {
+        dW[c] = sqdt * z[c];
+        W2[c] = (dW[c] * dW[c]) / sqdt;
+        W3[c] = (0.0f * (dW[c] * dW[c] * dW[c])) / dt;
+      }
+      const float tstg = TP::stage(t, 1.0f, dt);
+#pragma unroll
+      for (int c = 0; c < N; c++) x[c] = up[c] + (1.0f * f[c]) * dt + (1.0f * g[c]) * dW[c] + g[c] * W3[c];
+      degpu_f<float>(k1, x, p, tstg);
+#pragma unroll
+      for (int c = 0; c < N; c++) x[c] = up[c] + (1.0f * f[c]) * dt + (1.0f * g[c]) * sqdt + (0.0f * g[c]) * W2[c];
+      degpu_g<float>(g1, x, p, tstg);
+#pragma unroll
+      for (int c = 0; c < N; c++) x[c] = up[c] + (1.0f * f[c]) * dt + (-1.0f * g[c]) * sqdt + (0.0f * g[c]) * W2[c];
+      degpu_g<float>(g2, x, p, tstg);
+#pragma unroll
+      for (int c = 0; c < N; c++) {
+        u[c] = up[c] + (0.5f * f[c] + 0.5f * k1[c]) * dt;
+        u[c] = u[c] + ((0.5f * g[c]) * dW[c] + ((0.25f * dW[c] + -0.25f * sqdt) + 0.25f * W2[c]) * g1[c] +
+                       ((0.25f * dW[c] + 0.25f * sqdt) + -0.25f * W2[c]) * g2[c]);
+      }
+    }
+#else
 #pragma unroll
     for (int c = 0; c < N; c++) u[c] = up[c] + f[c] * dt + (sqdt * g[c]) * z[c];
+#endif
     t = TP::add(t, dt);
     if (!sa && P.save_everystep) {
       if (j - 1 < L) { for (int c = 0; c < N; c++) us[(j - 1) * N + c] = u[c]; ts[j - 1] = TP::out(t); }

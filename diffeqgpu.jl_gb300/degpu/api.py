@@ -86,6 +86,11 @@ class GPUEM(GPUSDEAlgorithm):
     alg_id, order = _lib.ALG_EM, 1
 
 
+class GPUSIEA(GPUSDEAlgorithm):
+    """Stochastic improved Euler, weak order 2, diagonal noise (gpu_siea_perform_step.jl)."""
+    alg_id, order = _lib.ALG_SIEA, 2
+
+
 def alg_order(alg) -> int:
     return alg.order
 

@@ -52,7 +52,7 @@
 #include "tableaus_gen.h"
 
 /* ------------------------------------------------------------------ constants */
-enum { ALG_TSIT5 = 0, ALG_VERN7 = 1, ALG_RB23 = 2, ALG_RODAS5P = 3, ALG_EM = 4, ALG_RODAS4 = 5, ALG_VERN9 = 6 };
+enum { ALG_TSIT5 = 0, ALG_VERN7 = 1, ALG_RB23 = 2, ALG_RODAS5P = 3, ALG_EM = 4, ALG_RODAS4 = 5, ALG_VERN9 = 6, ALG_SIEA = 7 };
 enum { RET_DEFAULT = 0, RET_SUCCESS = 1, RET_TERMINATED = 2, RET_DTMIN = 3, RET_MAXITERS = 4, RET_UNSTABLE = 5 };
 enum { JAC_AD = 0, JAC_ANALYTIC = 1, JAC_FINITEDIFF = 2 };
 enum {
@@ -1445,7 +1445,28 @@ static void em_one(int m, const oracle_cfg* cfg, long long idx, const float* u0,
     model_f<float>(m, f, up, p, t_f32(t));
     model_g(m, g, up, p);
     for (int b = 0; b < (N + 3) / 4; b++) normals4(cfg->seed, (uint32_t)(j - 2), (uint32_t)idx, (uint32_t)b, z + 4 * b);
-    for (int i = 0; i < N; i++) u[i] = up[i] + f[i] * dt + (sqdt * g[i]) * z[i];
+    if (cfg->alg == ALG_SIEA) { /* gpu_siea_perform_step.jl:48-139, coefficients :23-47 */
+      float dW[MAXN], W2[MAXN], W3[MAXN], x[MAXN], k1[MAXN], g1[MAXN], g2[MAXN];
+      for (int i = 0; i < N; i++) {
+        dW[i] = sqdt * z[i];
+        W2[i] = (dW[i] * dW[i]) / sqdt;
+        W3[i] = (0.0f * (dW[i] * dW[i] * dW[i])) / dt;
+      }
+      const float tstg = t_stage(t, 1.0f, dt);
+      for (int i = 0; i < N; i++) x[i] = up[i] + (1.0f * f[i]) * dt + (1.0f * g[i]) * dW[i] + g[i] * W3[i];
+      model_f<float>(m, k1, x, p, tstg);
+      for (int i = 0; i < N; i++) x[i] = up[i] + (1.0f * f[i]) * dt + (1.0f * g[i]) * sqdt + (0.0f * g[i]) * W2[i];
+      model_g(m, g1, x, p);
+      for (int i = 0; i < N; i++) x[i] = up[i] + (1.0f * f[i]) * dt + (-1.0f * g[i]) * sqdt + (0.0f * g[i]) * W2[i];
+      model_g(m, g2, x, p);
+      for (int i = 0; i < N; i++) {
+        u[i] = up[i] + (0.5f * f[i] + 0.5f * k1[i]) * dt;
+        u[i] = u[i] + ((0.5f * g[i]) * dW[i] + ((0.25f * dW[i] + -0.25f * sqdt) + 0.25f * W2[i]) * g1[i] +
+                       ((0.25f * dW[i] + 0.25f * sqdt) + -0.25f * W2[i]) * g2[i]);
+      }
+    } else {
+      for (int i = 0; i < N; i++) u[i] = up[i] + f[i] * dt + (sqdt * g[i]) * z[i];
+    }
     t = t_add(t, dt);
     if (!sa && cfg->save_everystep) {
       if (j - 1 < L) { for (int i = 0; i < N; i++) US(j - 1)[i] = u[i]; ts[j - 1] = t_out(t); }
@@ -1491,7 +1512,7 @@ int oracle_solve(int model, long long B, const float* u0, const float* p, const 
     const float* pi = p + (size_t)i * P;
     const double* tsp = tspan + 2 * (size_t)i;
     float* usi = us + (size_t)i * L * N;
-    if (cfg->alg == ALG_EM) {
+    if (cfg->alg == ALG_EM || cfg->alg == ALG_SIEA) {
       if (cfg->time_f64) em_one<DF>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (double*)ts + (size_t)i * L, usi, retcode);
       else em_one<float>(model, cfg, i, u0 + (size_t)i * N, pi, tsp, (float*)ts + (size_t)i * L, usi, retcode);
     } else {

@@ -38,7 +38,7 @@ def gpu_solve(degpu, model, alg, u0, p, tspan, tt, *, adaptive, dt, saveat=None,
     B = u0.shape[0]
     tsp = np.broadcast_to(np.asarray(tspan, dtype=tt), (B, 2))
     probs = degpu.DeviceProblems(f, u0, p, tsp, tt, torch.device("cuda", 0))
-    a = getattr(degpu, ALGS[alg])() if alg != "em" else degpu.GPUEM()
+    a = {"em": degpu.GPUEM, "siea": degpu.GPUSIEA}[alg]() if alg in ("em", "siea") else getattr(degpu, ALGS[alg])()
     r = degpu.api._solve_device(probs, a, adaptive, dt=dt, saveat=saveat, save_everystep=save_everystep, **kw)
     torch.cuda.synchronize()
     return (r.ts.cpu().numpy(), r.us.cpu().numpy(), r.retcode.cpu().numpy(), r.naccept.cpu().numpy(),
@@ -199,6 +199,40 @@ def test_em_bit_parity(degpu_mod, oracle_mod):
                                            L=len(sa), saveat=sa.astype(np.float32).astype(np.float64), seed=1234)
     assert_bit_equal(us, ous, "us")
     assert (rc == 1).all()
+
+
+@pytest.mark.parametrize("tt", [np.float32, np.float64])
+def test_siea_bit_parity(degpu_mod, oracle_mod, tt):
+    """GPUSIEA (gpu_siea_perform_step.jl) on GBM: parity mode reproduces the oracle's paths
+    bit for bit (saveat linear interpolation, both time types)."""
+    B = 1000
+    u0 = np.full((B, 1), 0.1, np.float32)
+    p = np.tile(np.array([1.5, 0.2], np.float32), (B, 1))
+    sa = np.linspace(0, 1, 11)
+    ts, us, rc, _, _ = gpu_solve(degpu_mod, "gbm", "siea", u0, p, (0, 1), tt, adaptive=False,
+                                 dt=float(np.float32(1 / 64)), saveat=sa, mode="parity", seed=99)
+    ots, ous, orc, _, _ = oracle_mod.solve("gbm", "siea", u0, p, [0, 1], adaptive=False, dt=float(np.float32(1 / 64)),
+                                           L=len(sa), saveat=sa.astype(tt).astype(np.float64), seed=99,
+                                           time_f64=tt == np.float64)
+    assert_bit_equal(us, ous, "us")
+    assert (rc == 1).all()
+
+
+def test_siea_weak_order(degpu_mod):
+    """gpu_sde_convergence.jl:34-45: weak order of GPUSIEA on du = 1.5 u dt + 0.01 u dW,
+    E[u(1)] = 0.1 e^1.5, dts 1/64..1/16 -- |order - 2.1| < 0.4 (10^6 paths, fast mode)."""
+    B = 1_000_000
+    u0 = np.full((B, 1), 0.1, np.float32)
+    p = np.tile(np.array([1.5, 0.01], np.float32), (B, 1))
+    exact = 0.1 * np.exp(1.5)
+    dts = [1 / 64, 1 / 32, 1 / 16]
+    errs = []
+    for dt in dts:
+        _, us, rc, _, _ = gpu_solve(degpu_mod, "gbm", "siea", u0, p, (0, 1), np.float32, adaptive=False,
+                                    dt=float(np.float32(dt)), save_everystep=False, mode="fast", seed=1234)
+        errs.append(abs(us[:, 1, 0].astype(np.float64).mean() - exact))
+    order = np.polyfit(np.log(dts), np.log(errs), 1)[0]
+    assert abs(order - 2.1) < 0.4, (errs, order)
 
 
 def test_em_weak_order_and_mean(degpu_mod):

@@ -214,6 +214,23 @@ def test_empirical_order(oracle_mod, alg, dts, lo, hi):
     assert lo <= np.mean(obs) <= hi, (errs, obs)
 
 
+def test_siea_weak_order(oracle_mod):
+    """GPUSIEA restatement: weak order ~2 on du = 1.5 u dt + 0.01 u dW (the reference's
+    gpu_sde_convergence.jl:34-45 bound |order - 2.1| < 0.4), 2*10^5 paths."""
+    B = 200_000
+    u0 = np.full((B, 1), 0.1, np.float32)
+    p = np.tile(np.array([1.5, 0.01], np.float32), (B, 1))
+    exact = 0.1 * np.exp(1.5)
+    dts = [1 / 32, 1 / 16, 1 / 8]
+    errs = []
+    for dt in dts:
+        _, us, _, _, _ = oracle_mod.solve("gbm", "siea", u0, p, [0.0, 1.0], adaptive=False, dt=float(np.float32(dt)), L=2,
+                                          seed=1234)
+        errs.append(abs(us[:, 1, 0].astype(np.float64).mean() - exact))
+    order = np.polyfit(np.log(dts), np.log(errs), 1)[0]
+    assert abs(order - 2.1) < 0.4, (errs, order)
+
+
 def test_em_weak_order(oracle_mod):
     """EM on du = 1.5 u dt + 0.01 u dW: weak error of E[u(1)] ~ O(dt) (order 1 +- 0.15,
     gpu_sde_convergence.jl:32)."""
