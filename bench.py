@@ -248,7 +248,7 @@ def extra_configs(args, dev, flush):
     ref2, _ = oracle.vern9("robertson", u02[idx2].astype(np.float64), k[idx2].astype(np.float64), 0.0, np.array([1e5]),
                            rtol=1e-10, atol=1e-14, method="rodas5p")
     for name, alg in (("rosenbrock23", degpu.GPURosenbrock23()), ("rodas5p", degpu.GPURodas5P()),
-                      ("rodas4", degpu.GPURodas4())):
+                      ("rodas4", degpu.GPURodas4()), ("kvaerno5", degpu.GPUKvaerno5())):
         def run2():
             holder["r"] = degpu.api._solve_device(pr2, alg, True, dt=1e-3, saveat=sa2, abstol=1e-7, reltol=1e-4)
         ms = time_solve(run2)

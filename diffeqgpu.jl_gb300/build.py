@@ -101,6 +101,7 @@ CHECKS = [  # (alg, driver, time type, parity, model, extra defines) compiled by
     (0, 0, "float", 1, "lorenz", ""), (0, 1, "double", 0, "lorenz", ""), (0, 2, "double", 0, "lorenz", ""),
     (1, 2, "double", 0, "lorenz", ""), (2, 2, "double", 0, "lorenz", ""), (3, 2, "double", 0, "lorenz", ""),
     (3, 1, "double", 1, "lorenz", ""), (5, 2, "double", 0, "lorenz", ""), (6, 2, "double", 0, "lorenz", ""),
+    (8, 2, "double", 0, "lorenz", ""), (9, 1, "float", 1, "lorenz", ""),
     # tstops + callbacks: continuous (bouncing ball) and discrete (decay) sets
     (0, 2, "double", 0, "ball", "-DDEGPU_NCCB=2 -DDEGPU_TSTOPS=1"),
     # SDE driver: Euler-Maruyama and SIEA on geometric Brownian motion

@@ -366,7 +366,7 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   if (!f || !pr || !o || !out) return fail(DEGPU_E_INVALID, "null argument");
   if (pr->B < 0) return fail(DEGPU_E_INVALID, "negative trajectory count");
   if (pr->B > 0x7fffffffLL) return fail(DEGPU_E_INVALID, "more than 2^31-1 trajectories in one call; split into batches");
-  if (o->alg < 0 || o->alg > 7) return fail(DEGPU_E_INVALID, "unknown algorithm");
+  if (o->alg < 0 || o->alg > 9) return fail(DEGPU_E_INVALID, "unknown algorithm");
   if (is_sde_alg(o->alg) && adaptive)
     return fail(DEGPU_E_UNSUPPORTED, o->alg == DEGPU_ALG_EM ? "Adaptive time-stepping is not supported yet with GPUEM."
                                                             : "Adaptive time-stepping is not supported yet with GPUSIEA.");
@@ -397,9 +397,11 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   else if (o->jac == DEGPU_JAC_AD) { k.jac = 0; k.tgrad = 0; }
   else if (o->jac == DEGPU_JAC_FINITEDIFF) { k.jac = 2; k.tgrad = 2; }
   else return fail(DEGPU_E_INVALID, "jac");
-  const bool rosenbrock = o->alg == DEGPU_ALG_ROSENBROCK23 || o->alg == DEGPU_ALG_RODAS5P || o->alg == DEGPU_ALG_RODAS4;
-  if (!rosenbrock) { k.jac = 0; k.tgrad = 0; }
-  k.refine = rosenbrock && !k.parity ? 1 : 0;
+  // algorithms that build Jacobians and solve linear systems: Rosenbrock and ESDIRK (Newton)
+  const bool implicit = o->alg == DEGPU_ALG_ROSENBROCK23 || o->alg == DEGPU_ALG_RODAS5P || o->alg == DEGPU_ALG_RODAS4 ||
+                        o->alg == DEGPU_ALG_KVAERNO3 || o->alg == DEGPU_ALG_KVAERNO5;
+  if (!implicit) { k.jac = 0; k.tgrad = 0; }
+  k.refine = implicit && !k.parity ? 1 : 0;
   degpu_kparams& P = rq->kp;
   memset(&P, 0, sizeof P);
   P.u0 = pr->u0;

@@ -5,7 +5,8 @@
 // defines, per translation unit:
 //   DEGPU_N, DEGPU_P        state / parameter dimensions
 //   DEGPU_TT                time type (float: the reference's Float32 tspan; double: FP64 time)
-//   DEGPU_ALG               0 Tsit5, 1 Vern7, 2 Rosenbrock23, 3 Rodas5P, 4 EM, 5 Rodas4, 6 Vern9, 7 SIEA
+//   DEGPU_ALG               0 Tsit5, 1 Vern7, 2 Rosenbrock23, 3 Rodas5P, 4 EM, 5 Rodas4, 6 Vern9, 7 SIEA,
+//                           8 Kvaerno3, 9 Kvaerno5
 //   DEGPU_DRIVER            0 fixed step, 1 adaptive (one trajectory per thread),
 //                           2 adaptive persistent (warp refill + work stealing), 3 EM
 //   DEGPU_PARITY            1: no FMA (set by --fmad=false), portable pow, Cramer solves
@@ -113,6 +114,12 @@ constexpr int ORDER = 4;
 #elif DEGPU_ALG == 6
 constexpr int NK = 10;
 constexpr int ORDER = 9;
+#elif DEGPU_ALG == 8
+constexpr int NK = 2;
+constexpr int ORDER = 3;
+#elif DEGPU_ALG == 9
+constexpr int NK = 2;
+constexpr int ORDER = 5;
 #else
 constexpr int NK = 1;
 constexpr int ORDER = 1;
@@ -157,6 +164,8 @@ __constant__ float c_tsit5[TS_COUNT] = {
 #define V9(n) c_vern9[VERN9_##n]
 #define V9X(n) c_vern9x[VERN9X_##n]
 #define V9I(n) c_vern9i[VERN9I_##n]
+#define K3(n) c_kvaerno3[KVAERNO3_##n]
+#define K5(n) c_kvaerno5[KVAERNO5_##n]
 
 // ------------------------------------------------------------------ small helpers
 DEGPU_DEV float tstage(Time t, float c, float dt) { return TP::stage(t, c, dt); }
@@ -1112,7 +1121,168 @@ DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
 }
 #endif
 
-#if DEGPU_ALG <= 3 || DEGPU_ALG == 5 || DEGPU_ALG == 6
+// ------------------------------------------------------------------ Kvaerno3 / Kvaerno5 (gpu_kvaerno{3,5}_perform_step.jl)
+// ESDIRK methods: each implicit stage solved by the GPU Newton iteration of the reference,
+// Hermite dense output from k1 and k2 = z_last / dt.
+#if DEGPU_ALG == 8 || DEGPU_ALG == 9
+// nlsolve (nlsolve/utils.jl:1-26) with the W of build_J_W (nlsolve/type.jl:129-140):
+// Newton on z for  z = dt f(tmp + γ z, t + c dt), with W = -I + (γ dt) J(tmp + γ z) rebuilt
+// every iteration, at most 30 iterations, stopping once the RMS of dt f(tmp + γ z) - z
+// is below 100 eps(Float32).  f at the new iterate, evaluated for that test, is the next
+// iteration's f (the reference evaluates it a second time; same bits).
+DEGPU_DEV void build_w(LinSys& S, const float* J, float gdt) {
+#pragma unroll
+  for (int j = 0; j < N; j++)
+#pragma unroll
+    for (int i = 0; i < N; i++) S.W[i + N * j] = (i == j) ? gdt * J[i + N * j] + -1.0f : gdt * J[i + N * j];
+#if !(DEGPU_PARITY || DEGPU_N > 3)
+  S.factor();
+#endif
+}
+DEGPU_DEV void nlsolve(const Lane& L, float* z, const float* tmp, float gam, float c, Time tn, float dtn) {
+  const float tc = TP::stage(tn, c, dtn);
+  const float gdt = gam * dtn;
+  float x[N], fx[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) x[i] = tmp[i] + gam * z[i];
+  rhs(fx, x, L.p, tc);
+#pragma unroll 1
+  for (int it = 0; it < 30; it++) {  // kept rolled: seven call sites of a 30-iteration body
+    float J[N * N], r[N], dz[N];
+    jacobian(J, x, L.p, tc);
+    LinSys S;
+    build_w(S, J, gdt);
+#pragma unroll
+    for (int i = 0; i < N; i++) r[i] = dtn * fx[i] - z[i];
+    S.solve(r, dz);
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      z[i] = z[i] - dz[i];
+      x[i] = tmp[i] + gam * z[i];
+    }
+    rhs(fx, x, L.p, tc);
+    float ss = 0.0f;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      const float e = dtn * fx[i] - z[i];
+      ss = (i == 0) ? e * e : ss + e * e;
+    }
+    if (sqrtf(ss / (float)N) < 1.1920928955078125e-05f) break;  // diffeqgpunorm < 100 eps(Float32)
+  }
+}
+DEGPU_DEV void begin_step(Lane& L, bool first) {
+#if DEGPU_DRIVER == 0
+  // fixed step: k1 = integ.k1 (f(u, p, t) of the previous step) unless u was modified (:26-31)
+  if (first) rhs(L.k[0], L.uprev, L.p, TP::f32(L.t));
+#else
+  // adaptive: k1 = f(uprev, p, t) at every attempt (one evaluation per step suffices)
+  rhs(L.k[0], L.uprev, L.p, TP::f32(L.t));
+#endif
+}
+// adaptive error estimate: W at (u, t + dt) applied to the embedded combination (:185-196)
+DEGPU_DEV void sdirk_error(const Lane& L, const float* u, Time t, float dt, float gam, const float* e, float* err) {
+  float J[N * N];
+  jacobian(J, u, L.p, TP::stage(t, 1.0f, dt));
+  LinSys S;
+  build_w(S, J, gam * dt);
+  S.solve(e, err);
+}
+// The nonlinear solver's time and step: the attempt's when adaptive; the fixed-step driver
+// builds it after advancing integ.t, from integ.t and integ.dt (:34-38).
+template <bool ADAPTIVE>
+DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
+  const float* up = L.uprev;
+  const Time tn = ADAPTIVE ? t : L.t;
+  const float dtn = ADAPTIVE ? dt : L.dt;
+  float tmp[N], z1[N], z2[N], z3[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) z1[i] = dt * L.k[0][i];
+#if DEGPU_ALG == 8
+  const float g = K3(gamma);
+  float z4[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) { z2[i] = z1[i]; tmp[i] = up[i] + g * z1[i]; }
+  nlsolve(L, z2, tmp, g, g, tn, dtn);
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    z3[i] = K3(alpha31) * z1[i] + K3(alpha32) * z2[i];
+    tmp[i] = up[i] + K3(a31) * z1[i] + K3(a32) * z2[i];
+  }
+  nlsolve(L, z3, tmp, g, K3(c3), tn, dtn);
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    z4[i] = K3(a31) * z1[i] + K3(a32) * z2[i] + g * z3[i];  // yhat as the prediction
+    tmp[i] = up[i] + K3(a41) * z1[i] + K3(a42) * z2[i] + K3(a43) * z3[i];
+  }
+  nlsolve(L, z4, tmp, g, 1.0f, tn, dtn);
+#pragma unroll
+  for (int i = 0; i < N; i++) { u[i] = tmp[i] + g * z4[i]; L.k[1][i] = z4[i] / dt; }
+  if (ADAPTIVE) {
+    float e[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) e[i] = K3(btilde1) * z1[i] + K3(btilde2) * z2[i] + K3(btilde3) * z3[i] + K3(btilde4) * z4[i];
+    sdirk_error(L, u, t, dt, g, e, err);
+  }
+#else
+  const float g = K5(gamma);
+  float z4[N], z5[N], z6[N], z7[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) { z2[i] = z1[i]; tmp[i] = up[i] + g * z1[i]; }
+  nlsolve(L, z2, tmp, g, g, tn, dtn);
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    z3[i] = K5(alpha31) * z1[i] + K5(alpha32) * z2[i];
+    tmp[i] = up[i] + K5(a31) * z1[i] + K5(a32) * z2[i];
+  }
+  nlsolve(L, z3, tmp, g, K5(c3), tn, dtn);
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    z4[i] = K5(alpha41) * z1[i] + K5(alpha42) * z2[i] + K5(alpha43) * z3[i];
+    tmp[i] = up[i] + K5(a41) * z1[i] + K5(a42) * z2[i] + K5(a43) * z3[i];
+  }
+  nlsolve(L, z4, tmp, g, K5(c4), tn, dtn);
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    z5[i] = K5(alpha51) * z1[i] + K5(alpha52) * z2[i] + K5(alpha53) * z3[i];
+    tmp[i] = up[i] + K5(a51) * z1[i] + K5(a52) * z2[i] + K5(a53) * z3[i] + K5(a54) * z4[i];
+  }
+  nlsolve(L, z5, tmp, g, K5(c5), tn, dtn);
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    z6[i] = K5(alpha61) * z1[i] + K5(alpha62) * z2[i] + K5(alpha63) * z3[i];
+    tmp[i] = up[i] + K5(a61) * z1[i] + K5(a63) * z3[i] + K5(a64) * z4[i] + K5(a65) * z5[i];
+  }
+  nlsolve(L, z6, tmp, g, K5(c6), tn, dtn);
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    z7[i] = K5(a61) * z1[i] + K5(a63) * z3[i] + K5(a64) * z4[i] + K5(a65) * z5[i] + g * z6[i];
+    tmp[i] = up[i] + K5(a71) * z1[i] + K5(a73) * z3[i] + K5(a74) * z4[i] + K5(a75) * z5[i] + K5(a76) * z6[i];
+  }
+  nlsolve(L, z7, tmp, g, 1.0f, tn, dtn);
+#pragma unroll
+  for (int i = 0; i < N; i++) { u[i] = tmp[i] + g * z7[i]; L.k[1][i] = z7[i] / dt; }
+  if (ADAPTIVE) {
+    float e[N];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+      e[i] = K5(btilde1) * z1[i] + K5(btilde3) * z3[i] + K5(btilde4) * z4[i] + K5(btilde5) * z5[i] + K5(btilde6) * z6[i] + K5(btilde7) * z7[i];
+    sdirk_error(L, u, t, dt, g, e, err);
+  }
+#endif
+  // fixed step: integ.k1 = f(u, p, t) (the step's start time; :83-86), the next step's k1
+  if (!ADAPTIVE) rhs(L.k[0], u, L.p, TP::f32(t));
+}
+// default Hermite interpolation (nonstiff/interpolants.jl:1-21), evaluated without FMA in
+// parity mode
+DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
+  const float a = 1.0f - th, b = th * (th - 1.0f), c = 1.0f - 2.0f * th, d = (th - 1.0f) * dt, e = th * dt;
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    out[i] = (a * L.uprev[i] + th * L.u[i]) + b * ((c * (L.u[i] - L.uprev[i]) + d * L.k[0][i]) + e * L.k[1][i]);
+}
+#endif
+
+#if DEGPU_ALG <= 3 || DEGPU_ALG == 5 || DEGPU_ALG == 6 || DEGPU_ALG == 8 || DEGPU_ALG == 9
 // ------------------------------------------------------------------ driver pieces (kernels.jl)
 // Loop-invariant kernel parameters copied into registers once per thread (reading them
 // through a reference to the parameter block inside the step loop costs a constant-bank
@@ -1607,7 +1777,7 @@ DEGPU_DEV void lane_finish(Lane& L, const Io& io, int i) {
   if (io.P.naccept) io.P.naccept[i] = L.naccept;
   if (io.P.nreject) io.P.nreject[i] = L.nreject;
 }
-#endif  // DEGPU_ALG <= 3 || DEGPU_ALG == 5 || DEGPU_ALG == 6
+#endif  // ODE algorithms
 
 }  // namespace degpu
 

@@ -7,7 +7,7 @@ the Python mirror of the reference's interface; there is no CPU fallback.
 from ._lib import DegpuError, RETCODE_NAMES, lib  # noqa: F401
 from .api import (  # noqa: F401
     CallbackSet, ContinuousCallback, DiscreteCallback, GPUContinuousCallback, GPUDiscreteCallback, LeftRootFind,
-    NoRootFind, RightRootFind, DeviceProblems, EnsembleGPUKernel, EnsembleProblem, EnsembleSolution, GPUEM, GPUSIEA, GPURodas4, GPURodas5, GPURodas5P,
+    NoRootFind, RightRootFind, DeviceProblems, EnsembleGPUKernel, EnsembleProblem, EnsembleSolution, GPUEM, GPUSIEA, GPUKvaerno3, GPUKvaerno5, GPURodas4, GPURodas5, GPURodas5P,
     GPURosenbrock23, GPUTsit5, GPUVern7, GPUVern9, LinRange, ODEFunction, ODEProblem, ODESolution, Range, SDEFunction,
     SDEProblem, adapt, alg_order, make_prob_compatible, normalize_saveat, remake, solve, vectorized_asolve,
     vectorized_solve,

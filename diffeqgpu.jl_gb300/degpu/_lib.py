@@ -8,7 +8,8 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libdegpu.so"
 
 OK, E_INVALID, E_COMPILE, E_CUDA, E_UNSUPPORTED = 0, -1, -2, -3, -4
-ALG_TSIT5, ALG_VERN7, ALG_ROSENBROCK23, ALG_RODAS5P, ALG_EM, ALG_RODAS4, ALG_VERN9, ALG_SIEA = range(8)
+(ALG_TSIT5, ALG_VERN7, ALG_ROSENBROCK23, ALG_RODAS5P, ALG_EM, ALG_RODAS4, ALG_VERN9, ALG_SIEA, ALG_KVAERNO3,
+ ALG_KVAERNO5) = range(10)
 TIME_F32, TIME_F64 = 0, 1
 MODE_FAST, MODE_PARITY = 0, 1
 DRIVER_AUTO, DRIVER_NAIVE, DRIVER_PERSISTENT = 0, 1, 2

@@ -78,6 +78,14 @@ class GPURodas4(GPUODEImplicitAlgorithm):
     alg_id, order = _lib.ALG_RODAS4, 4
 
 
+class GPUKvaerno3(GPUODEImplicitAlgorithm):
+    alg_id, order = _lib.ALG_KVAERNO3, 3
+
+
+class GPUKvaerno5(GPUODEImplicitAlgorithm):
+    alg_id, order = _lib.ALG_KVAERNO5, 5
+
+
 # The reference has no Rodas5 (non-P) tableau; GPURodas5 is Rodas5P's coefficients.
 GPURodas5 = GPURodas5P
 

@@ -49,6 +49,12 @@ def attempt_flops(alg: str, N: int, model: str, adaptive: bool = True) -> int:
         lu = 2 * N ** 3 // 3 + N * N
         solve = 2 * N * N
         return 21 + N * N + lu + 6 * solve + 6 * rhs + 78 * N + (5 * N + 14 if adaptive else 0)
+    if alg in ("kvaerno3", "kvaerno5"):
+        # per Newton iteration: J (AD ~ 3 rhs N), W, one solve, two rhs (counted as one: the
+        # test's f is the next iteration's), residual and norm; ~3 iterations per stage
+        stages = 3 if alg == "kvaerno3" else 6
+        it = 3 * rhs * N + 2 * N * N + (2 * N ** 3 // 3 + N * N) + 2 * N * N + rhs + 6 * N
+        return stages * 3 * it + (stages + 1) * 10 * N + (2 * N ** 3 // 3 + 5 * N * N + 5 * N + 14 if adaptive else 0)
     raise ValueError(alg)
 
 
@@ -59,6 +65,8 @@ def step_flops(alg: str, N: int, model: str) -> int:
         return rhs
     if alg in ("rosenbrock23", "rodas5p", "rodas4"):
         return 3 * rhs * N  # Jacobian by forward-mode AD ~ N dual sweeps
+    if alg in ("kvaerno3", "kvaerno5"):
+        return rhs  # k1
     return 0
 
 
@@ -74,6 +82,8 @@ def interp_flops(alg: str, N: int, model: str) -> int:
         return 8 + 5 * N
     if alg == "rodas4":
         return 1 + 7 * N
+    if alg in ("kvaerno3", "kvaerno5"):
+        return 8 + 12 * N  # Hermite
     return 8 + 9 * N
 
 

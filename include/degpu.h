@@ -40,6 +40,8 @@ extern "C" {
 #define DEGPU_ALG_RODAS4 5 /* GPURodas4 (gpukernel_algorithms.jl:137, perform_step/gpu_rodas4_perform_step.jl) */
 #define DEGPU_ALG_VERN9 6  /* GPUVern9 (gpukernel_algorithms.jl:83, perform_step/gpu_vern9_perform_step.jl) */
 #define DEGPU_ALG_SIEA 7   /* GPUSIEA, weak order 2 SDE (gpukernel_algorithms.jl:266, perform_step/gpu_siea_perform_step.jl) */
+#define DEGPU_ALG_KVAERNO3 8 /* GPUKvaerno3 (gpukernel_algorithms.jl:187, perform_step/gpu_kvaerno3_perform_step.jl) */
+#define DEGPU_ALG_KVAERNO5 9 /* GPUKvaerno5 (gpukernel_algorithms.jl:212, perform_step/gpu_kvaerno5_perform_step.jl) */
 
 #define DEGPU_TIME_F32 0 /* Float32 tspan: every operation is the reference's Float32 one */
 #define DEGPU_TIME_F64 1 /* FP64 time accumulation / end detection, FP32 state */

@@ -37,9 +37,32 @@ TABLES = [
     ("vern9i", "src/ensemblegpukernel/tableaus/verner_tableaus.jl", "Vern9InterpolationCoefficients"),
     ("rodas5p", "src/ensemblegpukernel/tableaus/rodas_tableaus.jl", "Rodas5PTableau"),
     ("rodas4", "src/ensemblegpukernel/tableaus/rodas_tableaus.jl", "Rodas4Tableau"),
+    ("kvaerno3", "src/ensemblegpukernel/tableaus/kvaerno_tableaus.jl", "Kvaerno3Tableau"),
+    ("kvaerno5", "src/ensemblegpukernel/tableaus/kvaerno_tableaus.jl", "Kvaerno5Tableau"),
 ]
 
-ASSIGN = re.compile(r"^\s*([A-Za-z_γ][A-Za-z0-9_γ]*)\s*=\s*(-?)\s*convert\(\s*T2?\s*,\s*([-+0-9.eE]+)\s*\)\s*$")
+
+def derived(tab: str, entries):
+    """Coefficients the reference computes from others instead of writing them as literals
+    (kvaerno_tableaus.jl:33-38 and :159), evaluated in Float32 like the Float32 tableau:
+    Kvaerno3 btilde4 = -γ and its Hermite predictor weights α31, α32 with c2 = 2γ,
+    θ = c3/c2; Kvaerno5 btilde7 = -γ."""
+    f = np.float32
+    d = dict(entries)
+    if tab == "kvaerno3":
+        g, c3 = f(d["gamma"]), f(d["c3"])
+        c2 = f(2) * g
+        th = c3 / c2
+        th2 = th * th
+        w = (f(6) * th * (f(1) - th)) / c2 * g
+        a31 = (f(1) + (f(-4) * th + f(3) * th2)) + w
+        a32 = (f(-2) * th + f(3) * th2) + w
+        return [("btilde4", float(-g)), ("alpha31", float(a31)), ("alpha32", float(a32))]
+    if tab == "kvaerno5":
+        return [("btilde7", float(-f(d["gamma"])))]
+    return []
+
+ASSIGN = re.compile(r"^\s*([A-Za-z_γα][A-Za-z0-9_γα]*)\s*=\s*(-?)\s*convert\(\s*T2?\s*,\s*([-+0-9.eE]+)\s*\)\s*(#.*)?$")
 
 
 def parse_function(path: Path, fname: str):
@@ -60,7 +83,7 @@ def parse_function(path: Path, fname: str):
             break
         m = ASSIGN.match(ln)
         if m:
-            name = m.group(1).replace("γ", "gamma")
+            name = m.group(1).replace("γ", "gamma").replace("α", "alpha")
             v = float(m.group(3))
             out.append((name, -v if m.group(2) else v))  # `-convert(T, x)`: negation is exact
     return out, start + 1, end + 1
@@ -85,7 +108,7 @@ def main():
     ]
     dev_lines = [
         "// Generated by oracle/gen_tableaus.py -- do not edit.",
-        "// Method coefficients (Verner 7(6) and 9(8), Rodas5P, Rodas4) rounded once from their published FP64",
+        "// Method coefficients (Verner 7(6) and 9(8), Rodas5P, Rodas4, Kvaerno3/5) rounded once from their published FP64",
         "// values to FP32, exactly as Julia's convert(Float32, ::Float64) does in the reference",
         "// (see per-table citations).  They live in constant memory and are read as",
         "// constant-bank operands by the stage arithmetic.",
@@ -94,6 +117,7 @@ def main():
     ]
     for tab, rel, fname in TABLES:
         entries, l0, l1 = parse_function(ref / rel, fname)
+        entries = entries + derived(tab, entries)
         cite = f"{rel}:{l0}-{l1} ({fname})"
         names = [n for n, _ in entries]
         oracle_lines.append(f"/* {cite} */")

@@ -52,7 +52,7 @@
 #include "tableaus_gen.h"
 
 /* ------------------------------------------------------------------ constants */
-enum { ALG_TSIT5 = 0, ALG_VERN7 = 1, ALG_RB23 = 2, ALG_RODAS5P = 3, ALG_EM = 4, ALG_RODAS4 = 5, ALG_VERN9 = 6, ALG_SIEA = 7 };
+enum { ALG_TSIT5 = 0, ALG_VERN7 = 1, ALG_RB23 = 2, ALG_RODAS5P = 3, ALG_EM = 4, ALG_RODAS4 = 5, ALG_VERN9 = 6, ALG_SIEA = 7, ALG_KVAERNO3 = 8, ALG_KVAERNO5 = 9 };
 enum { RET_DEFAULT = 0, RET_SUCCESS = 1, RET_TERMINATED = 2, RET_DTMIN = 3, RET_MAXITERS = 4, RET_UNSTABLE = 5 };
 enum { JAC_AD = 0, JAC_ANALYTIC = 1, JAC_FINITEDIFF = 2 };
 enum {
@@ -312,7 +312,7 @@ static Tsit5Tab make_tsit5() {
 static const Tsit5Tab TS5 = make_tsit5();
 
 static float V7[OR_VERN7_COUNT], V7X[OR_VERN7X_COUNT], V7I[OR_VERN7I_COUNT], R5P[OR_RODAS5P_COUNT], R4T[OR_RODAS4_COUNT];
-static float F9[OR_VERN9_COUNT], F9X[OR_VERN9X_COUNT], F9I[OR_VERN9I_COUNT];
+static float F9[OR_VERN9_COUNT], F9X[OR_VERN9X_COUNT], F9I[OR_VERN9I_COUNT], FK3[OR_KVAERNO3_COUNT], FK5[OR_KVAERNO5_COUNT];
 static int tabs_ready = 0;
 static void init_tabs() {
   if (tabs_ready) return;
@@ -327,6 +327,8 @@ static void init_tabs() {
       for (int i = 0; i < OR_VERN9_COUNT; i++) F9[i] = (float)OR_VERN9[i];
       for (int i = 0; i < OR_VERN9X_COUNT; i++) F9X[i] = (float)OR_VERN9X[i];
       for (int i = 0; i < OR_VERN9I_COUNT; i++) F9I[i] = (float)OR_VERN9I[i];
+      for (int i = 0; i < OR_KVAERNO3_COUNT; i++) FK3[i] = (float)OR_KVAERNO3[i];
+      for (int i = 0; i < OR_KVAERNO5_COUNT; i++) FK5[i] = (float)OR_KVAERNO5[i];
       tabs_ready = 1;
     }
   }
@@ -339,6 +341,8 @@ static void init_tabs() {
 #define F9C(n) F9[OR_VERN9_##n]
 #define F9XC(n) F9X[OR_VERN9X_##n]
 #define F9IC(n) F9I[OR_VERN9I_##n]
+#define K3C(n) FK3[OR_KVAERNO3_##n]
+#define K5C(n) FK5[OR_KVAERNO5_##n]
 
 /* ------------------------------------------------------------------ configuration */
 extern "C" {
@@ -575,7 +579,7 @@ static Ctrl make_ctrl(int order) {
   return c;
 }
 static int alg_order(int alg) {
-  return alg == ALG_TSIT5 ? 5 : alg == ALG_VERN7 ? 7 : alg == ALG_RB23 ? 2 : alg == ALG_RODAS5P ? 5 : alg == ALG_RODAS4 ? 4 : alg == ALG_VERN9 ? 9 : 1;
+  return alg == ALG_TSIT5 ? 5 : alg == ALG_VERN7 ? 7 : alg == ALG_RB23 ? 2 : alg == ALG_RODAS5P ? 5 : alg == ALG_RODAS4 ? 4 : alg == ALG_VERN9 ? 9 : alg == ALG_KVAERNO3 ? 3 : alg == ALG_KVAERNO5 ? 5 : 1;
 }
 
 /* PI controller decision, shared by every adaptive step! (e.g. gpu_tsit5_perform_step.jl:124-170).
@@ -1013,6 +1017,105 @@ static void rodas4_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt,
   }
 }
 
+/* ------------------------------------------------------------------ Kvaerno3 / Kvaerno5
+ * gpu_kvaerno3_perform_step.jl, gpu_kvaerno5_perform_step.jl with nlsolve (nlsolve/utils.jl:1-26)
+ * and W = -I + (γ dt) J from build_J_W (nlsolve/type.jl:129-140). */
+static void sdirk_w(int N, const float* J, float gdt, float* W) {
+  for (int j = 0; j < N; j++)
+    for (int i = 0; i < N; i++) W[i + N * j] = (i == j) ? gdt * J[i + N * j] + -1.0f : gdt * J[i + N * j];
+}
+template <class Tt>
+static void nlsolve_o(int m, int jacmode, int N, const float* p, float* z, const float* tmp, float gam, float c, Tt tn, float dtn) {
+  const float tc = t_stage(tn, c, dtn);
+  const float gdt = gam * dtn;
+  float x[MAXN], fx[MAXN], J[MAXN * MAXN], W[MAXN * MAXN], r[MAXN], dz[MAXN];
+  for (int i = 0; i < N; i++) x[i] = tmp[i] + gam * z[i];
+  model_f<float>(m, fx, x, p, tc);
+  for (int it = 0; it < 30; it++) {
+    compute_J(m, jacmode, N, J, x, p, tc);
+    sdirk_w(N, J, gdt, W);
+    for (int i = 0; i < N; i++) r[i] = dtn * fx[i] - z[i];
+    linear_solve(N, W, r, dz);
+    for (int i = 0; i < N; i++) { z[i] = z[i] - dz[i]; x[i] = tmp[i] + gam * z[i]; }
+    model_f<float>(m, fx, x, p, tc);
+    for (int i = 0; i < N; i++) r[i] = dtn * fx[i] - z[i];
+    if (ode_norm(r, N) < 1.1920928955078125e-05f) break; /* diffeqgpunorm < 100 eps(Float32) */
+  }
+}
+/* One attempt.  k1: the step's k1; tn/dtn: the nonlinear solver's time and step (the
+ * attempt's when adaptive; integ.t after the advance and integ.dt for fixed steps).
+ * Writes u, k2 = z_last / dt and, when adaptive, err. */
+template <class Tt>
+static void kvaerno_attempt(int m, int jacmode, int alg, Integ<Tt>& ig, const float* p, Tt t, float dt, Tt tn, float dtn,
+                            const float* k1, float* u, float* k2, float* err, int adaptive) {
+  const int N = ig.N;
+  const float* up = ig.uprev;
+  float tmp[MAXN], z1[MAXN], z2[MAXN], z3[MAXN], z4[MAXN], z5[MAXN], z6[MAXN], z7[MAXN], e[MAXN], zl[MAXN];
+  float g;
+  for (int i = 0; i < N; i++) z1[i] = dt * k1[i];
+  if (alg == ALG_KVAERNO3) {
+    g = K3C(gamma);
+    for (int i = 0; i < N; i++) { z2[i] = z1[i]; tmp[i] = up[i] + g * z1[i]; }
+    nlsolve_o(m, jacmode, N, p, z2, tmp, g, g, tn, dtn);
+    for (int i = 0; i < N; i++) { z3[i] = K3C(alpha31) * z1[i] + K3C(alpha32) * z2[i]; tmp[i] = up[i] + K3C(a31) * z1[i] + K3C(a32) * z2[i]; }
+    nlsolve_o(m, jacmode, N, p, z3, tmp, g, K3C(c3), tn, dtn);
+    for (int i = 0; i < N; i++) {
+      z4[i] = K3C(a31) * z1[i] + K3C(a32) * z2[i] + g * z3[i];
+      tmp[i] = up[i] + K3C(a41) * z1[i] + K3C(a42) * z2[i] + K3C(a43) * z3[i];
+    }
+    nlsolve_o(m, jacmode, N, p, z4, tmp, g, 1.0f, tn, dtn);
+    for (int i = 0; i < N; i++) {
+      zl[i] = z4[i];
+      e[i] = K3C(btilde1) * z1[i] + K3C(btilde2) * z2[i] + K3C(btilde3) * z3[i] + K3C(btilde4) * z4[i];
+    }
+  } else {
+    g = K5C(gamma);
+    for (int i = 0; i < N; i++) { z2[i] = z1[i]; tmp[i] = up[i] + g * z1[i]; }
+    nlsolve_o(m, jacmode, N, p, z2, tmp, g, g, tn, dtn);
+    for (int i = 0; i < N; i++) { z3[i] = K5C(alpha31) * z1[i] + K5C(alpha32) * z2[i]; tmp[i] = up[i] + K5C(a31) * z1[i] + K5C(a32) * z2[i]; }
+    nlsolve_o(m, jacmode, N, p, z3, tmp, g, K5C(c3), tn, dtn);
+    for (int i = 0; i < N; i++) {
+      z4[i] = K5C(alpha41) * z1[i] + K5C(alpha42) * z2[i] + K5C(alpha43) * z3[i];
+      tmp[i] = up[i] + K5C(a41) * z1[i] + K5C(a42) * z2[i] + K5C(a43) * z3[i];
+    }
+    nlsolve_o(m, jacmode, N, p, z4, tmp, g, K5C(c4), tn, dtn);
+    for (int i = 0; i < N; i++) {
+      z5[i] = K5C(alpha51) * z1[i] + K5C(alpha52) * z2[i] + K5C(alpha53) * z3[i];
+      tmp[i] = up[i] + K5C(a51) * z1[i] + K5C(a52) * z2[i] + K5C(a53) * z3[i] + K5C(a54) * z4[i];
+    }
+    nlsolve_o(m, jacmode, N, p, z5, tmp, g, K5C(c5), tn, dtn);
+    for (int i = 0; i < N; i++) {
+      z6[i] = K5C(alpha61) * z1[i] + K5C(alpha62) * z2[i] + K5C(alpha63) * z3[i];
+      tmp[i] = up[i] + K5C(a61) * z1[i] + K5C(a63) * z3[i] + K5C(a64) * z4[i] + K5C(a65) * z5[i];
+    }
+    nlsolve_o(m, jacmode, N, p, z6, tmp, g, K5C(c6), tn, dtn);
+    for (int i = 0; i < N; i++) {
+      z7[i] = K5C(a61) * z1[i] + K5C(a63) * z3[i] + K5C(a64) * z4[i] + K5C(a65) * z5[i] + g * z6[i];
+      tmp[i] = up[i] + K5C(a71) * z1[i] + K5C(a73) * z3[i] + K5C(a74) * z4[i] + K5C(a75) * z5[i] + K5C(a76) * z6[i];
+    }
+    nlsolve_o(m, jacmode, N, p, z7, tmp, g, 1.0f, tn, dtn);
+    for (int i = 0; i < N; i++) {
+      zl[i] = z7[i];
+      e[i] = K5C(btilde1) * z1[i] + K5C(btilde3) * z3[i] + K5C(btilde4) * z4[i] + K5C(btilde5) * z5[i] + K5C(btilde6) * z6[i] + K5C(btilde7) * z7[i];
+    }
+  }
+  for (int i = 0; i < N; i++) { u[i] = tmp[i] + g * zl[i]; k2[i] = zl[i] / dt; }
+  if (adaptive) {
+    float J[MAXN * MAXN], W[MAXN * MAXN];
+    compute_J(m, jacmode, N, J, u, p, t_stage(t, 1.0f, dt));
+    sdirk_w(N, J, g * dt, W);
+    linear_solve(N, W, e, err);
+  }
+}
+
+/* default Hermite interpolation (nonstiff/interpolants.jl:1-21) */
+template <class Tt>
+static void hermite_interp(const Integ<Tt>& ig, float th, float dt, float* out) {
+  const float a = 1.0f - th, b = th * (th - 1.0f), c = 1.0f - 2.0f * th, d = (th - 1.0f) * dt, e = th * dt;
+  for (int i = 0; i < ig.N; i++)
+    out[i] = (a * ig.uprev[i] + th * ig.u[i]) + b * ((c * (ig.u[i] - ig.uprev[i]) + d * ig.k[0][i]) + e * ig.k[1][i]);
+}
+
 /* ------------------------------------------------------------------ interpolation (savevalues!) */
 template <class Tt>
 static void interpolate(int m, int alg, const Integ<Tt>& ig, const float* p, float th, float dt, float* out) {
@@ -1027,6 +1130,8 @@ static void interpolate(int m, int alg, const Integ<Tt>& ig, const float* p, flo
     } break;
     case ALG_VERN7: vern7_interp(m, ig, p, th, dt, out); break;
     case ALG_VERN9: vern9_interp(m, ig, p, th, dt, out); break;
+    case ALG_KVAERNO3:
+    case ALG_KVAERNO5: hermite_interp(ig, th, dt, out); break;
     case ALG_RB23: { /* nonstiff/interpolants.jl:389-399 */
       const float d = 1.0f / (2.0f + sqrtf(2.0f));
       float c1 = th * (1.0f - th) / (1.0f - 2.0f * d);
@@ -1301,6 +1406,14 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
         compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, t_f32(t));
         compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, t_f32(t));
         rodas5p_attempt(m, ig, p, t, dt, u, k8, ig.k);
+      } else if (alg == ALG_KVAERNO3 || alg == ALG_KVAERNO5) {
+        /* FSAL k1 = integ.k1 unless u was modified; the nonlinear solver takes integ.t (already
+         * advanced) and integ.dt (gpu_kvaerno3_perform_step.jl:26-38) */
+        float k1[MAXN], err[MAXN];
+        if (ig.u_modified) { model_f<float>(m, k1, ig.uprev, p, t_f32(t)); ig.u_modified = 0; }
+        else for (int i = 0; i < N; i++) k1[i] = ig.k[0][i];
+        kvaerno_attempt(m, cfg->jac, alg, ig, p, t, dt, ig.t, ig.dt, k1, u, ig.k[1], err, 0);
+        model_f<float>(m, ig.k[0], u, p, t_f32(t)); /* integ.k1 = f(u, p, t) (:83-86) */
       } else if (alg == ALG_RODAS4) {
         float k6[MAXN];
         compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, t_f32(t));
@@ -1316,6 +1429,7 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
         if (ig.u_modified) { model_f<float>(m, k1, ig.uprev, p, t_f32(t)); ig.u_modified = 0; }
         else for (int i = 0; i < N; i++) k1[i] = ig.k[6][i];
       }
+      if (alg == ALG_KVAERNO3 || alg == ALG_KVAERNO5) model_f<float>(m, k1, ig.uprev, p, t_f32(t)); /* k1 = f(uprev, p, t) */
       if (alg == ALG_RODAS5P || alg == ALG_RODAS4) { /* J, dT once per step, outside the reject loop */
         compute_J(m, cfg->jac, N, ig.J, ig.uprev, p, t_f32(t));
         compute_tgrad(m, cfg->jac, N, ig.dT, ig.uprev, p, t_f32(t));
@@ -1339,6 +1453,9 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
             err[i] = dt * (F9C(btilde1) * kk[0][i] + F9C(btilde8) * kk[1][i] + F9C(btilde9) * kk[2][i] + F9C(btilde10) * kk[3][i] + F9C(btilde11) * kk[4][i] + F9C(btilde12) * kk[5][i] + F9C(btilde13) * kk[6][i] + F9C(btilde14) * kk[7][i] + F9C(btilde15) * kk[8][i] + F9C(btilde16) * kk[9][i]);
         } else if (alg == ALG_RB23) {
           rb23_attempt(m, cfg->jac, ig, p, t, dt, u, kk[0], kk[1], err, 1);
+        } else if (alg == ALG_KVAERNO3 || alg == ALG_KVAERNO5) {
+          for (int i = 0; i < N; i++) kk[0][i] = k1[i];
+          kvaerno_attempt(m, cfg->jac, alg, ig, p, t, dt, t, dt, k1, u, kk[1], err, 1);
         } else if (alg == ALG_RODAS4) { /* error estimate is k6 */
           rodas4_attempt(m, ig, p, t, dt, u, err, kk);
         } else { /* Rodas5P: error estimate is k8 */
@@ -1346,7 +1463,8 @@ static void solve_one(int m, const oracle_cfg* cfg, long long idx, const float* 
         }
         EEst = scaled_norm(err, ig.uprev, u, N, ig.abstol, ig.reltol);
         if (controller(ig, C, EEst, dt, t)) {
-          int ns = alg == ALG_TSIT5 ? 7 : (alg == ALG_VERN7 || alg == ALG_VERN9) ? 10 : (alg == ALG_RB23 || alg == ALG_RODAS4) ? 2 : 3;
+          int ns = alg == ALG_TSIT5 ? 7 : (alg == ALG_VERN7 || alg == ALG_VERN9) ? 10
+                   : (alg == ALG_RB23 || alg == ALG_RODAS4 || alg == ALG_KVAERNO3 || alg == ALG_KVAERNO5) ? 2 : 3;
           for (int s = 0; s < ns; s++) for (int i = 0; i < N; i++) ig.k[s][i] = kk[s][i];
           for (int i = 0; i < N; i++) ig.u[i] = u[i];
           /* not snapped to tf: stop at the next tstop, u = integ(tstop) (:157-167) */

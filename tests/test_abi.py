@@ -45,7 +45,7 @@ def test_nvrtc_compiles_callback_kernels(degpu_mod):
                       ("decay", degpu_mod.CallbackSet(degpu_mod.DiscreteCallback(0), degpu_mod.DiscreteCallback(2)))):
         f = degpu_mod.ODEFunction.builtin(model)
         st, keep = cs.cstruct()
-        for alg in ("GPUTsit5", "GPUVern7", "GPURosenbrock23", "GPURodas5P", "GPURodas4", "GPUVern9"):
+        for alg in ("GPUTsit5", "GPUVern7", "GPURosenbrock23", "GPURodas5P", "GPURodas4", "GPUVern9", "GPUKvaerno3", "GPUKvaerno5"):
             for adaptive in (0, 1):
                 o = _opts(degpu_mod, getattr(degpu_mod, alg)(), tt=np.float32, mode="parity")
                 o.callbacks = ctypes.addressof(st)
@@ -83,7 +83,8 @@ def _opts(degpu_mod, alg, tt=np.float64, **kw):
     return degpu_mod.api._options(alg, tt, dt=kw.pop("dt", 0.1), **kw)
 
 
-@pytest.mark.parametrize("alg", ["GPUTsit5", "GPUVern7", "GPURosenbrock23", "GPURodas5P", "GPURodas4", "GPUVern9"])
+@pytest.mark.parametrize("alg", ["GPUTsit5", "GPUVern7", "GPURosenbrock23", "GPURodas5P", "GPURodas4", "GPUVern9",
+                                 "GPUKvaerno3", "GPUKvaerno5"])
 @pytest.mark.parametrize("mode", ["fast", "parity"])
 def test_nvrtc_compiles_every_algorithm(degpu_mod, alg, mode, tmp_path, monkeypatch):
     """NVRTC (sm_103a) compiles stepper + driver + right-hand side for each algorithm and

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 EPS32 = float(np.finfo(np.float32).eps)
 ALGS = {"tsit5": "GPUTsit5", "vern7": "GPUVern7", "rosenbrock23": "GPURosenbrock23", "rodas5p": "GPURodas5P",
-        "rodas4": "GPURodas4", "vern9": "GPUVern9"}
+        "rodas4": "GPURodas4", "vern9": "GPUVern9", "kvaerno3": "GPUKvaerno3", "kvaerno5": "GPUKvaerno5"}
 
 
 def run_pair(degpu, oracle, model, alg, u0, p, tspan, tt, *, adaptive, dt, callbacks, tstops=None, saveat=None,
@@ -144,7 +144,7 @@ def test_terminate_and_rootfind_modes(degpu_mod, oracle_mod):
         check_parity(g, o)
 
 
-@pytest.mark.parametrize("alg", ["rosenbrock23", "rodas5p", "rodas4"])
+@pytest.mark.parametrize("alg", ["rosenbrock23", "rodas5p", "rodas4", "kvaerno3", "kvaerno5"])
 @pytest.mark.parametrize("adaptive", [False, True])
 def test_stiff_bouncing_ball_parity(degpu_mod, oracle_mod, alg, adaptive):
     """stiff_ode/gpu_ode_continuous_callbacks.jl: tspan (0, 16.5), dt 0.1f0."""
@@ -160,7 +160,8 @@ def test_stiff_bouncing_ball_parity(degpu_mod, oracle_mod, alg, adaptive):
 
 
 # ----------------------------------------------------------------------------- discrete
-@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p", "rodas4", "vern9"])
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p", "rodas4", "vern9", "kvaerno3",
+                                 "kvaerno5"])
 def test_discrete_tstops_parity(degpu_mod, oracle_mod, alg):
     """gpu_ode_discrete_callbacks.jl: condition t == 2.4f0 with tstops [2.4f0], dt 1f0; the
     dt 0.01f0 / tstops [4.0f0] truncation case; CallbackSet at 2.4 and 4.0 with saveat [0, 6]
@@ -181,6 +182,11 @@ def test_discrete_tstops_parity(degpu_mod, oracle_mod, alg):
     for c in cases:
         g, o = run_pair(degpu_mod, oracle_mod, "decay", alg, u0, p, (0.0, 10.0), np.float32, **c)
         check_parity(g, o)
+        if alg.startswith("kvaerno") and not c["adaptive"]:
+            # the reference's fixed-step ESDIRKs solve a step clipped to a tstop with the
+            # unclipped dt in their Newton iteration (gpu_kvaerno3_perform_step.jl:34-38), so
+            # only parity is checked there
+            continue
         # exact: u = 10 e^{-t} plus 10 e^{-(t - s)} for each event s <= t
         ev = [2.4 if cb.fn == 0 else 4.0 for cb in c["callbacks"]]
         ts, us = g[0][0], g[1][0, :, 0]
@@ -189,7 +195,8 @@ def test_discrete_tstops_parity(degpu_mod, oracle_mod, alg):
             t = float(ts[l])
             # a row saved at an event time holds the value before the affect
             exact = 10 * np.exp(-t) + sum(10 * np.exp(-(t - s)) for s in ev if s < t - 1e-5)
-            rt = {"tsit5": 5e-3, "vern7": 5e-3, "rosenbrock23": 0.15, "rodas5p": 2e-2, "rodas4": 2e-2, "vern9": 5e-3}[alg]  # fixed dt 1 on u' = -u
+            rt = {"tsit5": 5e-3, "vern7": 5e-3, "rosenbrock23": 0.15, "rodas5p": 2e-2, "rodas4": 2e-2, "vern9": 5e-3,
+                  "kvaerno3": 0.1, "kvaerno5": 2e-2}[alg]  # fixed dt 1 on u' = -u
             assert abs(us[l] - exact) < rt * max(1.0, exact), (c, l, t, us[l], exact)
 
 

@@ -180,7 +180,8 @@ def test_rodas5p_f64_matches_radau(oracle_mod):
 
 
 # ----------------------------------------------------------------------------- known answers / orders
-@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p", "rodas4", "vern9"])
+@pytest.mark.parametrize("alg", ["tsit5", "vern7", "rosenbrock23", "rodas5p", "rodas4", "vern9", "kvaerno3",
+                                 "kvaerno5"])
 def test_decay_known_answer(oracle_mod, alg):
     """u' = -u: adaptive solution at the saveat grid vs exp(-t)."""
     B = 4
@@ -188,7 +189,7 @@ def test_decay_known_answer(oracle_mod, alg):
     p = np.ones((B, 1), np.float32)
     sa = np.linspace(0, 1, 11)
     tol = {"rosenbrock23": 1e-4, "tsit5": 1e-5, "vern7": 1e-5, "rodas5p": 1e-5, "rodas4": 1e-5,
-           "vern9": 1e-4}[alg]  # Vern9's dense output cancels coefficients up to 1e4 in FP32
+           "vern9": 1e-4, "kvaerno3": 1e-5, "kvaerno5": 1e-5}[alg]  # Vern9's dense output cancels coefficients up to 1e4 in FP32
     ts, us, rc, _, _ = oracle_mod.solve("decay", alg, u0, p, [0, 1], adaptive=True, dt=0.01, L=11, saveat=sa,
                                         abstol=1e-8, reltol=1e-8)
     assert (rc == 1).all()
@@ -198,7 +199,9 @@ def test_decay_known_answer(oracle_mod, alg):
 @pytest.mark.parametrize("alg,dts,lo,hi", [("tsit5", [1.0, 0.5, 0.25], 4.6, 6.2), ("vern7", [2.0, 1.6], 6.3, 9.5),
                                             ("rosenbrock23", [0.2, 0.1, 0.05], 1.8, 2.3),
                                             ("rodas5p", [2.0, 1.0], 4.5, 6.5), ("rodas4", [1.0, 0.5, 0.25], 3.7, 4.6),
-                                            ("vern9", [2.0, 1.6, 1.2], 7.5, 12.0)])
+                                            ("vern9", [2.0, 1.6, 1.2], 7.5, 12.0),
+                                            ("kvaerno3", [0.4, 0.2, 0.1], 2.6, 3.3),
+                                            ("kvaerno5", [1.6, 0.8, 0.4], 4.3, 5.7)])
 def test_empirical_order(oracle_mod, alg, dts, lo, hi):
     """Fixed-step convergence on the harmonic oscillator over (0, 32).  The oracle is FP32,
     whose round-off floor (~1e-6) hides high orders at small steps, so the step sizes stay
