@@ -106,9 +106,11 @@ CHECKS = [  # (alg, driver, time type, parity, model, extra defines) compiled by
     (0, 2, "double", 0, "ball", "-DDEGPU_NCCB=2 -DDEGPU_TSTOPS=1"),
     # SDE driver: Euler-Maruyama and SIEA on geometric Brownian motion
     (4, 3, "float", 1, "gbm", ""), (7, 3, "double", 0, "gbm", ""),
+    # mass matrix (Robertson DAE)
+    (2, 1, "float", 1, "robertson_dae", "-DDEGPU_MASS=1"), (3, 2, "double", 0, "robertson_dae", "-DDEGPU_MASS=1"),
     (1, 0, "float", 1, "decay", "-DDEGPU_NDCB=2 -DDEGPU_TSTOPS=1"),
 ]
-MODEL_DIMS = {"lorenz": (3, 3), "ball": (2, 1), "decay": (1, 1), "gbm": (1, 2)}
+MODEL_DIMS = {"lorenz": (3, 3), "ball": (2, 1), "decay": (1, 1), "gbm": (1, 2), "robertson_dae": (3, 3)}
 
 
 def check_kernels(verbose: bool = False) -> list[str]:

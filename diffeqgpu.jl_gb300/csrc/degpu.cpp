@@ -122,10 +122,11 @@ bool is_sde_alg(int alg) { return alg == DEGPU_ALG_EM || alg == DEGPU_ALG_SIEA; 
 struct KernelSpec {
   int alg, driver, tt, parity, jac, tgrad, refine;
   int tstops = 0, nccb = 0, ndcb = 0;  // tstops / callback set compiled into the kernel
+  int mass = 0;                        // constant mass matrix (DEGPU_RHS_HAS_MASS)
   std::string key() const {
     char b[160];
-    snprintf(b, sizeof b, "a%d_d%d_t%d_m%d_j%d_g%d_r%d_s%d_c%d_e%d", alg, driver, tt, parity, jac, tgrad, refine,
-             tstops, nccb, ndcb);
+    snprintf(b, sizeof b, "a%d_d%d_t%d_m%d_j%d_g%d_r%d_s%d_c%d_e%d_M%d", alg, driver, tt, parity, jac, tgrad, refine,
+             tstops, nccb, ndcb, mass);
     return b;
   }
 };
@@ -167,9 +168,9 @@ std::string build_source(const degpu_rhs_s* f, const KernelSpec& k) {
            "#define DEGPU_N %d\n#define DEGPU_P %d\n#define DEGPU_TT %s\n#define DEGPU_ALG %d\n"
            "#define DEGPU_DRIVER %d\n#define DEGPU_PARITY %d\n#define DEGPU_JAC %d\n#define DEGPU_TGRAD %d\n"
            "#define DEGPU_LINSOLVE_REFINE %d\n#define DEGPU_TIME_DF %d\n"
-           "#define DEGPU_TSTOPS %d\n#define DEGPU_NCCB %d\n#define DEGPU_NDCB %d\n",
+           "#define DEGPU_TSTOPS %d\n#define DEGPU_NCCB %d\n#define DEGPU_NDCB %d\n#define DEGPU_MASS %d\n",
            f->N, f->P, k.tt ? "double" : "float", k.alg, k.driver, k.parity, k.jac, k.tgrad, k.refine, k.tt,
-           k.tstops, k.nccb, k.ndcb);
+           k.tstops, k.nccb, k.ndcb, k.mass);
   std::string s = defs;
   // developer override of the drivers' launch bounds (register budget experiments)
   if (const char* lb = getenv("DEGPU_LB")) {
@@ -401,6 +402,11 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   const bool implicit = o->alg == DEGPU_ALG_ROSENBROCK23 || o->alg == DEGPU_ALG_RODAS5P || o->alg == DEGPU_ALG_RODAS4 ||
                         o->alg == DEGPU_ALG_KVAERNO3 || o->alg == DEGPU_ALG_KVAERNO5;
   if (!implicit) { k.jac = 0; k.tgrad = 0; }
+  if (f->flags & DEGPU_RHS_HAS_MASS) {
+    if (o->alg != DEGPU_ALG_ROSENBROCK23 && o->alg != DEGPU_ALG_RODAS4 && o->alg != DEGPU_ALG_RODAS5P)
+      return fail(DEGPU_E_UNSUPPORTED, "a mass matrix needs GPURosenbrock23, GPURodas4 or GPURodas5P");
+    k.mass = 1;
+  }
   k.refine = implicit && !k.parity ? 1 : 0;
   degpu_kparams& P = rq->kp;
   memset(&P, 0, sizeof P);
@@ -579,7 +585,8 @@ int degpu_rhs_create(const char* cuda_source, int n_state, int n_param, int flag
   if (!cuda_source || !out) return fail(DEGPU_E_INVALID, "null argument");
   if (n_state < 1 || n_state > 32) return fail(DEGPU_E_INVALID, "state dimension must be in [1, 32]");
   if (n_param < 0 || n_param > 64) return fail(DEGPU_E_INVALID, "parameter count must be in [0, 64]");
-  if (flags & ~(DEGPU_RHS_HAS_JAC | DEGPU_RHS_HAS_TGRAD | DEGPU_RHS_HAS_NOISE)) return fail(DEGPU_E_INVALID, "unknown flags");
+  if (flags & ~(DEGPU_RHS_HAS_JAC | DEGPU_RHS_HAS_TGRAD | DEGPU_RHS_HAS_NOISE | DEGPU_RHS_HAS_MASS))
+    return fail(DEGPU_E_INVALID, "unknown flags");
   auto* f = new degpu_rhs_s;
   f->src = cuda_source;
   f->N = n_state;

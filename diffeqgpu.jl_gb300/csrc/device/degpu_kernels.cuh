@@ -95,6 +95,11 @@ constexpr int NP = DEGPU_P > 0 ? DEGPU_P : 1;
 #define DEGPU_NDCB 0
 #endif
 #define DEGPU_CALLBACKS (DEGPU_NCCB > 0 || DEGPU_NDCB > 0)
+// DEGPU_MASS 1: the source defines degpu_mass(float* M), the constant mass matrix of the
+// ODEFunction (column-major); only the Rosenbrock methods take it, as in the reference
+#ifndef DEGPU_MASS
+#define DEGPU_MASS 0
+#endif
 
 #if DEGPU_ALG == 0
 constexpr int NK = 7;
@@ -190,6 +195,34 @@ DEGPU_DEV float scaled_norm(const float* e, const float* up, const float* u, flo
   }
   return sqrtf(s / (float)N);
 }
+
+#if DEGPU_MASS
+// mass_matrix * v, each row summed left to right
+DEGPU_DEV void mass_mul(const float* M, const float* v, float* out) {
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    float acc = M[i] * v[0];
+#pragma unroll
+    for (int j = 1; j < N; j++) acc = acc + M[i + N * j] * v[j];
+    out[i] = acc;
+  }
+}
+// linsolve_tmp = base + mass_matrix * (combination) of the Rodas stages
+#define MASS_LT(LT, BASE, COMBO)                                    \
+  {                                                                 \
+    float cv_[N], mv_[N];                                           \
+    _Pragma("unroll") for (int i = 0; i < N; i++) cv_[i] = (COMBO); \
+    mass_mul(Mm, cv_, mv_);                                         \
+    _Pragma("unroll") for (int i = 0; i < N; i++) LT[i] = (BASE) + mv_[i]; \
+  }
+#define MASS_DIAG(i, j) Mm[(i) + N * (j)]
+#define MASS_SETUP float Mm[N * N]; degpu_mass(Mm);
+#else
+#define MASS_LT(LT, BASE, COMBO) \
+  { _Pragma("unroll") for (int i = 0; i < N; i++) LT[i] = (BASE) + (COMBO); }
+#define MASS_DIAG(i, j) ((i) == (j) ? 1.0f : 0.0f)
+#define MASS_SETUP
+#endif
 
 // ------------------------------------------------------------------ Jacobian / tgrad
 // build_J_W / build_tgrad (nlsolve/type.jl:129-157): user function, else forward-mode
@@ -597,11 +630,12 @@ template <bool ADAPTIVE>
 DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
   const float d = 1.0f / (2.0f + sqrtf(2.0f));
   float gam = dt * d, dto2 = dt / 2.0f, dto6 = dt / 6.0f;
+  MASS_SETUP
   LinSys S;
 #pragma unroll
   for (int j = 0; j < N; j++)
 #pragma unroll
-    for (int i = 0; i < N; i++) S.W[i + N * j] = (i == j ? 1.0f : 0.0f) - gam * L.J[i + N * j];
+    for (int i = 0; i < N; i++) S.W[i + N * j] = MASS_DIAG(i, j) - gam * L.J[i + N * j];  // mass_matrix - γ J
 #if !(DEGPU_PARITY || DEGPU_N > 3)
   S.factor();
 #endif
@@ -614,8 +648,17 @@ DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
 #pragma unroll
   for (int i = 0; i < N; i++) tmp[i] = L.uprev[i] + dto2 * k1[i];
   rhs(F1, tmp, L.p, tstage(t, 1.0f, dto2));
+#if DEGPU_MASS
+  {  // F1 - mass_matrix * k1 (:57, :132)
+    float mk[N];
+    mass_mul(Mm, k1, mk);
+#pragma unroll
+    for (int i = 0; i < N; i++) rhsv[i] = F1[i] - mk[i];
+  }
+#else
 #pragma unroll
   for (int i = 0; i < N; i++) rhsv[i] = F1[i] - k1[i];
+#endif
   S.solve(rhsv, k2);
 #pragma unroll
   for (int i = 0; i < N; i++) { k2[i] = k2[i] + k1[i]; u[i] = L.uprev[i] + dt * k2[i]; }
@@ -623,8 +666,19 @@ DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
     const float e32 = 6.0f + sqrtf(2.0f);
     float F2[N], k3[N];
     rhs(F2, u, L.p, tstage(t, 1.0f, dt));
+#if DEGPU_MASS
+    {  // F2 - mass_matrix * (e32 k2 + 2 k1) + e32 F1 + 2 F0 + dt dT (:144-149)
+      float cv[N], mv[N];
+#pragma unroll
+      for (int i = 0; i < N; i++) cv[i] = e32 * k2[i] + 2.0f * k1[i];
+      mass_mul(Mm, cv, mv);
+#pragma unroll
+      for (int i = 0; i < N; i++) rhsv[i] = F2[i] - mv[i] + e32 * F1[i] + 2.0f * L.F0[i] + dt * L.dT[i];
+    }
+#else
 #pragma unroll
     for (int i = 0; i < N; i++) rhsv[i] = F2[i] - e32 * (k2[i] - F1[i]) - 2.0f * (k1[i] - L.F0[i]) + dt * L.dT[i];
+#endif
     S.solve(rhsv, k3);
 #pragma unroll
     for (int i = 0; i < N; i++) err[i] = dto6 * (k1[i] - 2.0f * k2[i] + k3[i]);
@@ -650,6 +704,7 @@ DEGPU_DEV void begin_step(Lane& L, bool) {
 template <bool ADAPTIVE>
 DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* uout, float* err) {
   const float* up = L.uprev;
+  MASS_SETUP
   float dtC21 = RP(C21) / dt, dtC31 = RP(C31) / dt, dtC32 = RP(C32) / dt, dtC41 = RP(C41) / dt, dtC42 = RP(C42) / dt, dtC43 = RP(C43) / dt;
   float dtC51 = RP(C51) / dt, dtC52 = RP(C52) / dt, dtC53 = RP(C53) / dt, dtC54 = RP(C54) / dt;
   float dtC61 = RP(C61) / dt, dtC62 = RP(C62) / dt, dtC63 = RP(C63) / dt, dtC64 = RP(C64) / dt, dtC65 = RP(C65) / dt;
@@ -662,7 +717,7 @@ DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* uout, float* err) {
 #pragma unroll
   for (int j = 0; j < N; j++)
 #pragma unroll
-    for (int i = 0; i < N; i++) S.W[i + N * j] = L.J[i + N * j] - (i == j ? 1.0f : 0.0f) * inv_dtg;
+    for (int i = 0; i < N; i++) S.W[i + N * j] = L.J[i + N * j] - MASS_DIAG(i, j) * inv_dtg;
 #if !(DEGPU_PARITY || DEGPU_N > 3)
   S.factor();
 #endif
@@ -680,44 +735,37 @@ DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* uout, float* err) {
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + RP(a21) * k1[i];
   rhs(du, u, L.p, tstage(t, RP(c2), dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd2 * L.dT[i] + dtC21 * k1[i];
+  MASS_LT(lt, du[i] + dtd2 * L.dT[i], dtC21 * k1[i]);
   SOLVE(k2);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + RP(a31) * k1[i] + RP(a32) * k2[i];
   rhs(du, u, L.p, tstage(t, RP(c3), dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd3 * L.dT[i] + (dtC31 * k1[i] + dtC32 * k2[i]);
+  MASS_LT(lt, du[i] + dtd3 * L.dT[i], (dtC31 * k1[i] + dtC32 * k2[i]));
   SOLVE(k3);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + RP(a41) * k1[i] + RP(a42) * k2[i] + RP(a43) * k3[i];
   rhs(du, u, L.p, tstage(t, RP(c4), dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd4 * L.dT[i] + (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]);
+  MASS_LT(lt, du[i] + dtd4 * L.dT[i], (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]));
   SOLVE(k4);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + RP(a51) * k1[i] + RP(a52) * k2[i] + RP(a53) * k3[i] + RP(a54) * k4[i];
   rhs(du, u, L.p, tstage(t, RP(c5), dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd5 * L.dT[i] + (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]);
+  MASS_LT(lt, du[i] + dtd5 * L.dT[i], (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]));
   SOLVE(k5);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + RP(a61) * k1[i] + RP(a62) * k2[i] + RP(a63) * k3[i] + RP(a64) * k4[i] + RP(a65) * k5[i];
   rhs(du, u, L.p, tstage(t, 1.0f, dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC63 * k3[i] + dtC64 * k4[i] + dtC65 * k5[i]);
+  MASS_LT(lt, du[i], (dtC61 * k1[i] + dtC62 * k2[i] + dtC63 * k3[i] + dtC64 * k4[i] + dtC65 * k5[i]));
   SOLVE(k6);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = u[i] + k6[i];
   rhs(du, u, L.p, tstage(t, 1.0f, dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC71 * k1[i] + dtC72 * k2[i] + dtC73 * k3[i] + dtC74 * k4[i] + dtC75 * k5[i] + dtC76 * k6[i]);
+  MASS_LT(lt, du[i], (dtC71 * k1[i] + dtC72 * k2[i] + dtC73 * k3[i] + dtC74 * k4[i] + dtC75 * k5[i] + dtC76 * k6[i]));
   SOLVE(k7);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = u[i] + k7[i];
   rhs(du, u, L.p, tstage(t, 1.0f, dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC81 * k1[i] + dtC82 * k2[i] + dtC83 * k3[i] + dtC84 * k4[i] + dtC85 * k5[i] + dtC86 * k6[i] + dtC87 * k7[i]);
+  MASS_LT(lt, du[i], (dtC81 * k1[i] + dtC82 * k2[i] + dtC83 * k3[i] + dtC84 * k4[i] + dtC85 * k5[i] + dtC86 * k6[i] + dtC87 * k7[i]));
   SOLVE(k8);
 #undef SOLVE
 #pragma unroll
@@ -748,6 +796,7 @@ DEGPU_DEV void begin_step(Lane& L, bool) {
 template <bool ADAPTIVE>
 DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* uout, float* err) {
   const float* up = L.uprev;
+  MASS_SETUP
   float dtC21 = R4(C21) / dt, dtC31 = R4(C31) / dt, dtC32 = R4(C32) / dt, dtC41 = R4(C41) / dt, dtC42 = R4(C42) / dt, dtC43 = R4(C43) / dt;
   float dtC51 = R4(C51) / dt, dtC52 = R4(C52) / dt, dtC53 = R4(C53) / dt, dtC54 = R4(C54) / dt;
   float dtC61 = R4(C61) / dt, dtC62 = R4(C62) / dt, dtC63 = R4(C63) / dt, dtC64 = R4(C64) / dt, dtC65 = R4(C65) / dt;
@@ -758,7 +807,7 @@ DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* uout, float* err) {
 #pragma unroll
   for (int j = 0; j < N; j++)
 #pragma unroll
-    for (int i = 0; i < N; i++) S.W[i + N * j] = L.J[i + N * j] - (i == j ? 1.0f : 0.0f) * inv_dtg;
+    for (int i = 0; i < N; i++) S.W[i + N * j] = L.J[i + N * j] - MASS_DIAG(i, j) * inv_dtg;
 #if !(DEGPU_PARITY || DEGPU_N > 3)
   S.factor();
 #endif
@@ -776,32 +825,27 @@ DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* uout, float* err) {
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + R4(a21) * k1[i];
   rhs(du, u, L.p, tstage(t, R4(c2), dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd2 * L.dT[i] + dtC21 * k1[i];
+  MASS_LT(lt, du[i] + dtd2 * L.dT[i], dtC21 * k1[i]);
   SOLVE(k2);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + R4(a31) * k1[i] + R4(a32) * k2[i];
   rhs(du, u, L.p, tstage(t, R4(c3), dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd3 * L.dT[i] + (dtC31 * k1[i] + dtC32 * k2[i]);
+  MASS_LT(lt, du[i] + dtd3 * L.dT[i], (dtC31 * k1[i] + dtC32 * k2[i]));
   SOLVE(k3);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + R4(a41) * k1[i] + R4(a42) * k2[i] + R4(a43) * k3[i];
   rhs(du, u, L.p, tstage(t, R4(c4), dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd4 * L.dT[i] + (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]);
+  MASS_LT(lt, du[i] + dtd4 * L.dT[i], (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]));
   SOLVE(k4);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = up[i] + R4(a51) * k1[i] + R4(a52) * k2[i] + R4(a53) * k3[i] + R4(a54) * k4[i];
   rhs(du, u, L.p, tstage(t, 1.0f, dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]);
+  MASS_LT(lt, du[i], (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]));
   SOLVE(k5);
 #pragma unroll
   for (int i = 0; i < N; i++) u[i] = u[i] + k5[i];
   rhs(du, u, L.p, tstage(t, 1.0f, dt));
-#pragma unroll
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC65 * k5[i] + dtC64 * k4[i] + dtC63 * k3[i]);
+  MASS_LT(lt, du[i], (dtC61 * k1[i] + dtC62 * k2[i] + dtC65 * k5[i] + dtC64 * k4[i] + dtC63 * k3[i]));
   SOLVE(k6);
 #undef SOLVE
 #pragma unroll

@@ -14,7 +14,7 @@ TIME_F32, TIME_F64 = 0, 1
 MODE_FAST, MODE_PARITY = 0, 1
 DRIVER_AUTO, DRIVER_NAIVE, DRIVER_PERSISTENT = 0, 1, 2
 JAC_AUTO, JAC_AD, JAC_FINITEDIFF = 0, 1, 2
-RHS_HAS_JAC, RHS_HAS_TGRAD, RHS_HAS_NOISE = 1, 2, 4
+RHS_HAS_JAC, RHS_HAS_TGRAD, RHS_HAS_NOISE, RHS_HAS_MASS = 1, 2, 4, 8
 RET_DEFAULT, RET_SUCCESS, RET_TERMINATED, RET_DTLESSTHANMIN, RET_MAXITERS, RET_UNSTABLE = range(6)
 RETCODE_NAMES = {0: "Default", 1: "Success", 2: "Terminated", 3: "DtLessThanMin", 4: "MaxIters", 5: "Unstable"}
 

@@ -131,17 +131,20 @@ class EnsembleGPUKernel(EnsembleKernelAlgorithm):
 class ODEFunction:
     """A right-hand side written in CUDA C (see include/degpu.h, degpu_rhs_create).
 
-    ODEFunction(source, nstate, nparam, jac=False, tgrad=False, noise=False)
+    ODEFunction(source, nstate, nparam, jac=False, tgrad=False, noise=False, mass_matrix=False)
     ODEFunction.builtin("lorenz")
+
+    mass_matrix=True: the source defines degpu_mass(float* M), the constant mass matrix
+    (ODEFunction's mass_matrix keyword; Rosenbrock methods only).
     """
 
     def __init__(self, source: str, nstate: int, nparam: int, *, jac: bool = False, tgrad: bool = False,
-                 noise: bool = False, name: str = "user"):
+                 noise: bool = False, mass_matrix: bool = False, name: str = "user"):
         self.source = source
         self.nstate = int(nstate)
         self.nparam = int(nparam)
         self.flags = (_lib.RHS_HAS_JAC if jac else 0) | (_lib.RHS_HAS_TGRAD if tgrad else 0) | \
-                     (_lib.RHS_HAS_NOISE if noise else 0)
+                     (_lib.RHS_HAS_NOISE if noise else 0) | (_lib.RHS_HAS_MASS if mass_matrix else 0)
         self.name = name
         self._handle = None
 

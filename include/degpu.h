@@ -69,6 +69,8 @@ extern "C" {
 #define DEGPU_RHS_HAS_JAC 1   /* source defines degpu_jac(float* J, const float* u, const float* p, float t), J column-major */
 #define DEGPU_RHS_HAS_TGRAD 2 /* source defines degpu_tgrad(float* dT, const float* u, const float* p, float t) */
 #define DEGPU_RHS_HAS_NOISE 4 /* source defines template<class T> degpu_g(T* g, const T* u, const float* p, T t) (diagonal noise) */
+#define DEGPU_RHS_HAS_MASS 8  /* source defines degpu_mass(float* M): the constant mass matrix (column-major),
+                                 taken by GPURosenbrock23 / GPURodas4 / GPURodas5P (ODEFunction mass_matrix) */
 
 typedef struct degpu_rhs_s degpu_rhs;
 typedef struct degpu_plan_s degpu_plan;

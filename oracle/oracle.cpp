@@ -57,7 +57,7 @@ enum { RET_DEFAULT = 0, RET_SUCCESS = 1, RET_TERMINATED = 2, RET_DTMIN = 3, RET_
 enum { JAC_AD = 0, JAC_ANALYTIC = 1, JAC_FINITEDIFF = 2 };
 enum {
   M_LORENZ = 0, M_ROBERTSON = 1, M_DECAY = 2, M_GROWTH = 3, M_LINEAR15 = 4,
-  M_GBM = 5, M_LORENZ_ADDNOISE = 6, M_OSC = 7, M_BALL = 8
+  M_GBM = 5, M_LORENZ_ADDNOISE = 6, M_OSC = 7, M_BALL = 8, M_ROBER_DAE = 9
 };
 #define MAXN 16
 #define MAXP 8
@@ -92,7 +92,9 @@ template <int NP> static inline Dual<NP> operator-(Dual<NP> b, float a) { Dual<N
  *   gbm        test/gpu_kernel_de/gpu_sde_convergence.jl:6-8           (f = p1 u, g = p2 u)
  *   lorenz+additive noise  test/gpu_kernel_de/gpu_sde_regression.jl:47-58
  *   osc        harmonic oscillator u1' = u2, u2' = -p1^2 u1 (non-chaotic known answer)
- *   ball       bouncing ball u1' = u2, u2' = -p1 (test/gpu_kernel_de/gpu_ode_continuous_callbacks.jl:6-10) */
+ *   ball       bouncing ball u1' = u2, u2' = -p1 (test/gpu_kernel_de/gpu_ode_continuous_callbacks.jl:6-10)
+ *   robertson_dae  Robertson with the constraint y1 + y2 + y3 = 1 and mass matrix diag(1,1,0)
+ *              (test/gpu_kernel_de/stiff_ode/gpu_ode_mass_matrix.jl:5-31) */
 struct ModelInfo { int N, P, has_jac, has_tgrad, is_sde; };
 static ModelInfo model_info(int m) {
   switch (m) {
@@ -105,6 +107,7 @@ static ModelInfo model_info(int m) {
     case M_LORENZ_ADDNOISE: return {3, 3, 0, 0, 1};
     case M_OSC: return {2, 1, 1, 1, 0};
     case M_BALL: return {2, 1, 0, 0, 0};
+    case M_ROBER_DAE: return {3, 3, 0, 0, 0};
   }
   return {0, 0, 0, 0, 0};
 }
@@ -130,6 +133,27 @@ static void model_f(int m, S* du, const S* u, const float* p, float t) {
     case M_GBM: du[0] = p[0] * u[0]; break;
     case M_OSC: { du[0] = u[1]; du[1] = -(p[0] * p[0]) * u[0]; } break;
     case M_BALL: { du[0] = u[1]; du[1] = S(-p[0]); } break;
+    case M_ROBER_DAE: {
+      du[0] = -p[0] * u[0] + p[2] * u[1] * u[2];
+      du[1] = p[0] * u[0] - p[1] * (u[1] * u[1]) - p[2] * u[1] * u[2];
+      du[2] = u[0] + u[1] + u[2] - 1.0f;
+    } break;
+  }
+}
+
+/* constant mass matrix (column-major) of the models that have one; returns 0 for M = I */
+static int model_mass(int m, float* M) {
+  if (m != M_ROBER_DAE) return 0;
+  for (int i = 0; i < 9; i++) M[i] = 0.0f;
+  M[0] = 1.0f; M[4] = 1.0f;
+  return 1;
+}
+/* mass_matrix * v, rows summed left to right */
+static void mass_mul(int N, const float* M, const float* v, float* out) {
+  for (int i = 0; i < N; i++) {
+    float acc = M[i] * v[0];
+    for (int j = 1; j < N; j++) acc = acc + M[i + N * j] * v[j];
+    out[i] = acc;
   }
 }
 
@@ -889,13 +913,17 @@ static void rb23_attempt(int m, int jacmode, Integ<Tt>& ig, const float* p, Tt t
   float gam = dt * d, dto2 = dt / 2.0f, dto6 = dt / 6.0f;
   compute_J(m, jacmode, N, J, ig.uprev, p, tf_);
   compute_tgrad(m, jacmode, N, dT, ig.uprev, p, tf_);
-  for (int j = 0; j < N; j++) for (int i = 0; i < N; i++) W[i + N * j] = (i == j ? 1.0f : 0.0f) - gam * J[i + N * j];
+  float Mm[MAXN * MAXN];
+  const int has_mass = model_mass(m, Mm);
+  for (int j = 0; j < N; j++)
+    for (int i = 0; i < N; i++) W[i + N * j] = (has_mass ? Mm[i + N * j] : (i == j ? 1.0f : 0.0f)) - gam * J[i + N * j];
   model_f<float>(m, F0, ig.uprev, p, tf_);
   for (int i = 0; i < N; i++) rhs[i] = F0[i] + gam * dT[i];
   linear_solve(N, W, rhs, k1);
   for (int i = 0; i < N; i++) tmp[i] = ig.uprev[i] + dto2 * k1[i];
   model_f<float>(m, F1, tmp, p, t_stage(t, 1.0f, dto2));
-  for (int i = 0; i < N; i++) rhs[i] = F1[i] - k1[i];
+  if (has_mass) { float mk[MAXN]; mass_mul(N, Mm, k1, mk); for (int i = 0; i < N; i++) rhs[i] = F1[i] - mk[i]; }
+  else for (int i = 0; i < N; i++) rhs[i] = F1[i] - k1[i];
   linear_solve(N, W, rhs, k2);
   for (int i = 0; i < N; i++) k2[i] = k2[i] + k1[i];
   for (int i = 0; i < N; i++) u[i] = ig.uprev[i] + dt * k2[i];
@@ -903,10 +931,30 @@ static void rb23_attempt(int m, int jacmode, Integ<Tt>& ig, const float* p, Tt t
   if (!adaptive) return;
   const float e32 = 6.0f + sqrtf(2.0f);
   model_f<float>(m, F2, u, p, t_stage(t, 1.0f, dt));
-  for (int i = 0; i < N; i++) rhs[i] = F2[i] - e32 * (k2[i] - F1[i]) - 2.0f * (k1[i] - F0[i]) + dt * dT[i];
+  if (has_mass) {
+    float cv[MAXN], mv[MAXN];
+    for (int i = 0; i < N; i++) cv[i] = e32 * k2[i] + 2.0f * k1[i];
+    mass_mul(N, Mm, cv, mv);
+    for (int i = 0; i < N; i++) rhs[i] = F2[i] - mv[i] + e32 * F1[i] + 2.0f * F0[i] + dt * dT[i];
+  } else {
+    for (int i = 0; i < N; i++) rhs[i] = F2[i] - e32 * (k2[i] - F1[i]) - 2.0f * (k1[i] - F0[i]) + dt * dT[i];
+  }
   linear_solve(N, W, rhs, k3);
   for (int i = 0; i < N; i++) err[i] = dto6 * (k1[i] - 2.0f * k2[i] + k3[i]);
 }
+
+/* linsolve_tmp = base + mass_matrix * (combination) of the Rodas stages */
+#define MASS_LT_O(LT, BASE, COMBO)                                             \
+  {                                                                            \
+    if (has_mass) {                                                            \
+      float cv_[MAXN], mv_[MAXN];                                              \
+      for (int i = 0; i < N; i++) cv_[i] = (COMBO);                            \
+      mass_mul(N, Mm, cv_, mv_);                                               \
+      for (int i = 0; i < N; i++) LT[i] = (BASE) + mv_[i];                     \
+    } else {                                                                   \
+      for (int i = 0; i < N; i++) LT[i] = (BASE) + (COMBO);                    \
+    }                                                                          \
+  }
 
 /* ------------------------------------------------------------------ Rodas5P */
 template <class Tt>
@@ -922,7 +970,10 @@ static void rodas5p_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt
   float dtgamma = dt * RPC(gamma);
   float W[MAXN * MAXN];
   float inv_dtg = 1.0f / dtgamma;
-  for (int j = 0; j < N; j++) for (int i = 0; i < N; i++) W[i + N * j] = J[i + N * j] - (i == j ? 1.0f : 0.0f) * inv_dtg;
+  float Mm[MAXN * MAXN];
+  const int has_mass = model_mass(m, Mm);
+  for (int j = 0; j < N; j++)
+    for (int i = 0; i < N; i++) W[i + N * j] = J[i + N * j] - (has_mass ? Mm[i + N * j] : (i == j ? 1.0f : 0.0f)) * inv_dtg;
   float du[MAXN], u[MAXN], lt[MAXN], neg[MAXN];
   float k1[MAXN], k2[MAXN], k3[MAXN], k4[MAXN], k5[MAXN], k6[MAXN], k7[MAXN], k8[MAXN];
   float tf_ = t_f32(t);
@@ -932,31 +983,31 @@ static void rodas5p_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt
   SOLVE(k1);
   for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a21) * k1[i];
   model_f<float>(m, du, u, p, tstage(t, RPC(c2), dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd2 * dT[i] + dtC21 * k1[i];
+  MASS_LT_O(lt, du[i] + dtd2 * dT[i], dtC21 * k1[i]);
   SOLVE(k2);
   for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a31) * k1[i] + RPC(a32) * k2[i];
   model_f<float>(m, du, u, p, tstage(t, RPC(c3), dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd3 * dT[i] + (dtC31 * k1[i] + dtC32 * k2[i]);
+  MASS_LT_O(lt, du[i] + dtd3 * dT[i], (dtC31 * k1[i] + dtC32 * k2[i]));
   SOLVE(k3);
   for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a41) * k1[i] + RPC(a42) * k2[i] + RPC(a43) * k3[i];
   model_f<float>(m, du, u, p, tstage(t, RPC(c4), dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd4 * dT[i] + (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]);
+  MASS_LT_O(lt, du[i] + dtd4 * dT[i], (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]));
   SOLVE(k4);
   for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a51) * k1[i] + RPC(a52) * k2[i] + RPC(a53) * k3[i] + RPC(a54) * k4[i];
   model_f<float>(m, du, u, p, tstage(t, RPC(c5), dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd5 * dT[i] + (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]);
+  MASS_LT_O(lt, du[i] + dtd5 * dT[i], (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]));
   SOLVE(k5);
   for (int i = 0; i < N; i++) u[i] = up[i] + RPC(a61) * k1[i] + RPC(a62) * k2[i] + RPC(a63) * k3[i] + RPC(a64) * k4[i] + RPC(a65) * k5[i];
   model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC63 * k3[i] + dtC64 * k4[i] + dtC65 * k5[i]);
+  MASS_LT_O(lt, du[i], (dtC61 * k1[i] + dtC62 * k2[i] + dtC63 * k3[i] + dtC64 * k4[i] + dtC65 * k5[i]));
   SOLVE(k6);
   for (int i = 0; i < N; i++) u[i] = u[i] + k6[i];
   model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC71 * k1[i] + dtC72 * k2[i] + dtC73 * k3[i] + dtC74 * k4[i] + dtC75 * k5[i] + dtC76 * k6[i]);
+  MASS_LT_O(lt, du[i], (dtC71 * k1[i] + dtC72 * k2[i] + dtC73 * k3[i] + dtC74 * k4[i] + dtC75 * k5[i] + dtC76 * k6[i]));
   SOLVE(k7);
   for (int i = 0; i < N; i++) u[i] = u[i] + k7[i];
   model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC81 * k1[i] + dtC82 * k2[i] + dtC83 * k3[i] + dtC84 * k4[i] + dtC85 * k5[i] + dtC86 * k6[i] + dtC87 * k7[i]);
+  MASS_LT_O(lt, du[i], (dtC81 * k1[i] + dtC82 * k2[i] + dtC83 * k3[i] + dtC84 * k4[i] + dtC85 * k5[i] + dtC86 * k6[i] + dtC87 * k7[i]));
   SOLVE(k8);
 #undef SOLVE
   for (int i = 0; i < N; i++) { uout[i] = u[i] + k8[i]; k8o[i] = k8[i]; }
@@ -981,7 +1032,10 @@ static void rodas4_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt,
   float dtgamma = dt * R4C(gamma);
   float W[MAXN * MAXN];
   float inv_dtg = 1.0f / dtgamma;
-  for (int j = 0; j < N; j++) for (int i = 0; i < N; i++) W[i + N * j] = J[i + N * j] - (i == j ? 1.0f : 0.0f) * inv_dtg;
+  float Mm[MAXN * MAXN];
+  const int has_mass = model_mass(m, Mm);
+  for (int j = 0; j < N; j++)
+    for (int i = 0; i < N; i++) W[i + N * j] = J[i + N * j] - (has_mass ? Mm[i + N * j] : (i == j ? 1.0f : 0.0f)) * inv_dtg;
   float du[MAXN], u[MAXN], lt[MAXN], neg[MAXN];
   float k1[MAXN], k2[MAXN], k3[MAXN], k4[MAXN], k5[MAXN], k6[MAXN];
   float tf_ = t_f32(t);
@@ -991,23 +1045,23 @@ static void rodas4_attempt(int m, Integ<Tt>& ig, const float* p, Tt t, float dt,
   SOLVE(k1);
   for (int i = 0; i < N; i++) u[i] = up[i] + R4C(a21) * k1[i];
   model_f<float>(m, du, u, p, tstage(t, R4C(c2), dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd2 * dT[i] + dtC21 * k1[i];
+  MASS_LT_O(lt, du[i] + dtd2 * dT[i], dtC21 * k1[i]);
   SOLVE(k2);
   for (int i = 0; i < N; i++) u[i] = up[i] + R4C(a31) * k1[i] + R4C(a32) * k2[i];
   model_f<float>(m, du, u, p, tstage(t, R4C(c3), dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd3 * dT[i] + (dtC31 * k1[i] + dtC32 * k2[i]);
+  MASS_LT_O(lt, du[i] + dtd3 * dT[i], (dtC31 * k1[i] + dtC32 * k2[i]));
   SOLVE(k3);
   for (int i = 0; i < N; i++) u[i] = up[i] + R4C(a41) * k1[i] + R4C(a42) * k2[i] + R4C(a43) * k3[i];
   model_f<float>(m, du, u, p, tstage(t, R4C(c4), dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + dtd4 * dT[i] + (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]);
+  MASS_LT_O(lt, du[i] + dtd4 * dT[i], (dtC41 * k1[i] + dtC42 * k2[i] + dtC43 * k3[i]));
   SOLVE(k4);
   for (int i = 0; i < N; i++) u[i] = up[i] + R4C(a51) * k1[i] + R4C(a52) * k2[i] + R4C(a53) * k3[i] + R4C(a54) * k4[i];
   model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]);
+  MASS_LT_O(lt, du[i], (dtC52 * k2[i] + dtC54 * k4[i] + dtC51 * k1[i] + dtC53 * k3[i]));
   SOLVE(k5);
   for (int i = 0; i < N; i++) u[i] = u[i] + k5[i];
   model_f<float>(m, du, u, p, t_stage(t, 1.0f, dt));
-  for (int i = 0; i < N; i++) lt[i] = du[i] + (dtC61 * k1[i] + dtC62 * k2[i] + dtC65 * k5[i] + dtC64 * k4[i] + dtC63 * k3[i]);
+  MASS_LT_O(lt, du[i], (dtC61 * k1[i] + dtC62 * k2[i] + dtC65 * k5[i] + dtC64 * k4[i] + dtC63 * k3[i]));
   SOLVE(k6);
 #undef SOLVE
   for (int i = 0; i < N; i++) { uout[i] = u[i] + k6[i]; k6o[i] = k6[i]; }

@@ -17,7 +17,7 @@ LIB_PATH = HERE / "_build" / "liboracle.so"
 
 ALG = {"tsit5": 0, "vern7": 1, "rosenbrock23": 2, "rodas5p": 3, "em": 4, "rodas4": 5, "vern9": 6, "siea": 7, "kvaerno3": 8, "kvaerno5": 9}
 MODEL = {"lorenz": 0, "robertson": 1, "decay": 2, "growth": 3, "linear15": 4,
-         "gbm": 5, "lorenz_addnoise": 6, "osc": 7, "ball": 8}
+         "gbm": 5, "lorenz_addnoise": 6, "osc": 7, "ball": 8, "robertson_dae": 9}
 JAC = {"ad": 0, "analytic": 1, "finitediff": 2}
 RET = {"default": 0, "success": 1, "terminated": 2, "dtmin": 3, "maxiters": 4, "unstable": 5}
 

@@ -68,11 +68,25 @@ def test_callback_validation(degpu_mod):
     assert degpu_mod.lib().degpu_rhs_check(f.handle(), ctypes.byref(o), 1, ctypes.byref(n)) == -1
 
 
+def test_mass_matrix_only_with_rosenbrock(degpu_mod):
+    """A mass matrix is accepted by the Rosenbrock methods and refused by the others."""
+    from degpu import _lib
+    f = degpu_mod.ODEFunction.builtin("robertson_dae")
+    assert f.flags & _lib.RHS_HAS_MASS
+    n = ctypes.c_longlong()
+    for alg in (degpu_mod.GPURosenbrock23(), degpu_mod.GPURodas4(), degpu_mod.GPURodas5P()):
+        _lib.check(degpu_mod.lib().degpu_rhs_check(f.handle(), ctypes.byref(_opts(degpu_mod, alg, mode="parity")), 1,
+                                                   ctypes.byref(n)))
+    for alg in (degpu_mod.GPUTsit5(), degpu_mod.GPUKvaerno5()):
+        assert degpu_mod.lib().degpu_rhs_check(f.handle(), ctypes.byref(_opts(degpu_mod, alg)), 1, ctypes.byref(n)) == -4
+        assert b"mass matrix" in degpu_mod.lib().degpu_last_error()
+
+
 def test_version_and_builtins(degpu_mod):
     assert degpu_mod.lib().degpu_version() == b"0.1.0"
     for name, (n, p) in {"lorenz": (3, 3), "robertson": (3, 3), "decay": (1, 1), "growth": (1, 1),
                          "linear15": (15, 1), "gbm": (1, 2), "lorenz_addnoise": (3, 3), "osc": (2, 1),
-                         "ball": (2, 1)}.items():
+                         "ball": (2, 1), "robertson_dae": (3, 3)}.items():
         f = degpu_mod.ODEFunction.builtin(name)
         assert (f.nstate, f.nparam) == (n, p)
     with pytest.raises(KeyError):

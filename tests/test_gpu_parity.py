@@ -175,6 +175,28 @@ def test_stiff_fast_mode_vs_fp64(degpu_mod, oracle_mod, alg):
     assert err.max() < tol, err.max()
 
 
+@pytest.mark.parametrize("alg,dt", [("rosenbrock23", 0.1), ("rodas4", 1e-3), ("rodas5p", 1e-3)])
+def test_mass_matrix_dae_parity(degpu_mod, oracle_mod, alg, dt):
+    """gpu_ode_mass_matrix.jl: Robertson DAE with mass matrix diag(1,1,0), 512 perturbed rate
+    sets: parity mode bit-identical to the oracle; fast mode within the reference's 8e-4 of
+    the FP64 ODE-form solution and on the constraint."""
+    u0, k = robertson_batch(512, seed=9)
+    sa = np.array([0.0, 1.0, 10.0, 100.0, 1e3, 1e4, 1e5])
+    ts, us, rc, na, nr = gpu_solve(degpu_mod, "robertson_dae", alg, u0, k, (0, 1e5), np.float32, adaptive=True, dt=dt,
+                                   saveat=sa, abstol=1e-5, reltol=1e-5, mode="parity")
+    ots, ous, orc, ona, onr = oracle_mod.solve("robertson_dae", alg, u0, k, [0, 1e5], adaptive=True, dt=dt,
+                                               L=len(sa), saveat=sa, abstol=1e-5, reltol=1e-5)
+    assert (rc == orc).all() and (na == ona).all()
+    assert_bit_equal(us, ous, "us")
+    ts, us, rc, _, _ = gpu_solve(degpu_mod, "robertson_dae", alg, u0, k, (0, 1e5), np.float64, adaptive=True, dt=dt,
+                                 saveat=sa, abstol=1e-5, reltol=1e-5, mode="fast")
+    ref, _ = oracle_mod.vern9("robertson", u0.astype(np.float64), k.astype(np.float64), 0.0, sa, rtol=1e-10,
+                              atol=1e-14, method="rodas5p")
+    assert (rc == 1).all()
+    assert np.abs(us - ref).max() < 8e-4
+    assert np.abs(us.sum(axis=2) - 1.0).max() < 1e-5
+
+
 def test_linear15_lu_path(degpu_mod, oracle_mod):
     """N = 15 exercises the partial-pivot LU solve (linsolve.jl:88-108) in both modes."""
     B = 64

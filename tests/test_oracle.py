@@ -325,3 +325,20 @@ def test_portable_pow_accuracy(oracle_mod):
         ref = xs.astype(np.float64) ** np.float64(y32)
         assert np.abs(got / ref - 1).max() < 4e-6
     assert oracle_mod.pm_powf(0.0, 0.14) == 0.0
+
+
+@pytest.mark.parametrize("alg,dt", [("rosenbrock23", 0.1), ("rodas4", 1e-3), ("rodas5p", 1e-3)])
+def test_mass_matrix_dae_robertson(oracle_mod, alg, dt):
+    """gpu_ode_mass_matrix.jl: Robertson as a DAE (mass matrix diag(1,1,0), constraint
+    y1 + y2 + y3 = 1), abstol = reltol = 1e-5: within the reference's 8e-4 of the FP64
+    solution of the ODE form, and on the constraint."""
+    k = np.array([[0.04, 3e7, 1e4]], np.float32)
+    u0 = np.array([[1, 0, 0]], np.float32)
+    sa = np.array([0.0, 1.0, 10.0, 100.0, 1e3, 1e4, 1e5])
+    ref, _ = oracle_mod.vern9("robertson", u0.astype(np.float64), k.astype(np.float64), 0.0, sa, rtol=1e-10,
+                              atol=1e-14, method="rodas5p")
+    ts, us, rc, _, _ = oracle_mod.solve("robertson_dae", alg, u0, k, [0, 1e5], adaptive=True, dt=dt, L=len(sa),
+                                        saveat=sa, abstol=1e-5, reltol=1e-5)
+    assert rc[0] == 1
+    assert np.abs(us[0] - ref[0]).max() < 8e-4
+    assert np.abs(us[0].sum(axis=1) - 1.0).max() < 1e-6
