@@ -577,7 +577,7 @@ def gpu_arm(args):
 
 
 # see the traffic note in gpu_arm
-TRAFFIC_BYTES_PER_TRAJ = (33.2e6 + 176.7e6) / 524288
+TRAFFIC_BYTES_PER_TRAJ = (37.9e6 + 183.0e6) / 524288
 
 
 def main():
