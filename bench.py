@@ -303,6 +303,24 @@ def extra_configs(args, dev, flush):
         "trajectories_per_s": B5 / (ms * 1e-3), "ms": ms, "attempts_per_traj": float((na + nr).mean()),
         "fp32_tflops": fl / (ms * 1e-3) / 1e12, "retcodes_ok": bool((r.retcode.cpu().numpy() == 1).all())}
 
+    # the public Python API end to end (degpu.solve on a bulk-built EnsembleProblem: host
+    # arrays in, page-locked host ts/us out, lazy per-trajectory solutions)
+    Bs = 1 << 20
+    u0s, ps = make_inputs(Bs, WORKLOAD["seed"] + 7)
+    prob_s = degpu.ODEProblem(f, u0s[0], WORKLOAD["tspan"], ps[0], time_type=np.float64)
+    ens_s = degpu.EnsembleProblem.from_arrays(prob_s, u0=u0s, p=ps)
+    kw_s = dict(trajectories=Bs, adaptive=True, dt=WORKLOAD["dt"], saveat=saveat_grid(), abstol=WORKLOAD["abstol"],
+                reltol=WORKLOAD["reltol"])
+    degpu.solve(ens_s, degpu.GPUTsit5(), degpu.EnsembleGPUKernel(dev.index), **kw_s)
+    walls = []
+    for _ in range(3):
+        w0 = time.perf_counter()
+        sol = degpu.solve(ens_s, degpu.GPUTsit5(), degpu.EnsembleGPUKernel(dev.index), **kw_s)
+        walls.append(time.perf_counter() - w0)
+    res["python_solve_api_1M"] = {"trajectories_per_s": Bs / min(walls), "ms": 1e3 * min(walls),
+                                  "retcodes_ok": bool((sol.retcodes == 1).all()), "n_solutions": len(sol),
+                                  "api": "degpu.solve(EnsembleProblem.from_arrays(...), GPUTsit5(), EnsembleGPUKernel(0))"}
+
     # bouncing balls with a continuous callback (ITP event location + affect): heights
     # U(5, 50), gravities U(5, 15), tspan (0, 12), 25 saved points, error against the exact bounce
     B4 = 1 << 20

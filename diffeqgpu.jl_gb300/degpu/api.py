@@ -735,12 +735,20 @@ def solve(ens: EnsembleProblem, alg, ensemblealg: EnsembleGPUKernel, *, trajecto
         r = _solve_device(dp, alg, adaptive, dt=dt, saveat=saveat, save_everystep=save_everystep,
                           abstol=abstol, reltol=reltol, traj_offset=b0, callback=callback, tstops=tstops, **kw)
         parts.append(r)
+    # gather: one page-locked host array per output, each batch copied into its rows with an
+    # asynchronous device-to-host copy (no per-batch host arrays, no concatenation)
+    def gather(name):
+        first = getattr(parts[0], name)
+        host = torch.empty((trajectories,) + tuple(first.shape[1:]), dtype=first.dtype, pin_memory=True)
+        row = 0
+        for r in parts:
+            a = getattr(r, name)
+            host[row:row + a.shape[0]].copy_(a, non_blocking=True)
+            row += a.shape[0]
+        return host
+    ts_h, us_h, rc_h, na_h, nr_h = (gather(n) for n in ("ts", "us", "retcode", "naccept", "nreject"))
     torch.cuda.synchronize(dev)
-    ts = np.concatenate([r.ts.cpu().numpy() for r in parts])
-    us = np.concatenate([r.us.cpu().numpy() for r in parts])
-    rc = np.concatenate([r.retcode.cpu().numpy() for r in parts])
-    na = np.concatenate([r.naccept.cpu().numpy() for r in parts])
-    nr = np.concatenate([r.nreject.cpu().numpy() for r in parts])
+    ts, us, rc, na, nr = (x.numpy() for x in (ts_h, us_h, rc_h, na_h, nr_h))
     elapsed = time.perf_counter() - tstart
     t0 = np.concatenate(t0s).astype(ts.dtype)
     sols = _LazySolutions(ts, us, t0, alg, ens.output_func, "ode")
