@@ -237,15 +237,19 @@ def EnsembleContext(i, sim_seed=None):
 
 @dataclass
 class EnsembleProblem:
-    """EnsembleProblem(prob; prob_func, output_func, safetycopy).
+    """EnsembleProblem(prob; prob_func, output_func, reduction, u_init, safetycopy).
 
     prob_func(prob, ctx) -> prob is called once per trajectory (src/solve.jl:186-202).
-    For large ensembles, EnsembleProblem.from_arrays builds the batch in bulk."""
+    reduction(u, batch, I) -> (u, converged) folds each batch of (output_func-mapped)
+    solutions into u, starting from u_init (src/solve.jl:97-164).  For large ensembles,
+    EnsembleProblem.from_arrays builds the batch in bulk."""
     prob: ODEProblem
     prob_func: Optional[Callable] = None
     output_func: Optional[Callable] = None
     safetycopy: bool = False
     arrays: Optional[dict] = None
+    reduction: Optional[Callable] = None
+    u_init: Any = None
 
     @classmethod
     def from_arrays(cls, prob: ODEProblem, *, u0=None, p=None, tspan=None, saveat=None):
@@ -437,10 +441,13 @@ class DeviceProblems:
         self.Tt = Tt
         self.kind = kind
         tdt = torch.float32 if Tt == np.float32 else torch.float64
-        self.u0 = torch.as_tensor(np.ascontiguousarray(u0, dtype=np.float32), device=device)
-        self.p = torch.as_tensor(np.ascontiguousarray(p, dtype=np.float32), device=device)
-        self.tspan = torch.as_tensor(np.ascontiguousarray(tspan, dtype=Tt), device=device).to(tdt)
-        self.saveat = None if saveat is None else torch.as_tensor(np.ascontiguousarray(saveat, dtype=Tt), device=device)
+        def dev_array(a, dt):  # contiguous, writable host copy only when needed (read-only views warn)
+            a = np.ascontiguousarray(a, dtype=dt)
+            return torch.as_tensor(a if a.flags.writeable else a.copy(), device=device)
+        self.u0 = dev_array(u0, np.float32)
+        self.p = dev_array(p, np.float32)
+        self.tspan = dev_array(tspan, Tt).to(tdt)
+        self.saveat = None if saveat is None else dev_array(saveat, Tt)
         self.B = self.u0.shape[0]
 
     def __len__(self):
@@ -628,8 +635,9 @@ class _LazySolutions(Sequence):
     """Per-trajectory ODESolution views built on demand (the reference builds them eagerly
     in a host loop, src/solve.jl:256-283)."""
 
-    def __init__(self, ts, us, t0, alg, output_func, probs_kind):
+    def __init__(self, ts, us, t0, alg, output_func, probs_kind, offset=0):
         self.ts, self.us, self.t0, self.alg, self.output_func = ts, us, t0, alg, output_func
+        self.offset = offset  # global index of row 0 (EnsembleContext sim_id)
 
     def __len__(self):
         return self.ts.shape[0]
@@ -647,7 +655,7 @@ class _LazySolutions(Sequence):
         sol = ODESolution(ts[:idx], self.us[i, :idx], alg=self.alg,
                           retcode=RETCODE_SUCCESS if idx == ts.shape[0] else RETCODE_TERMINATED)
         if self.output_func is not None:
-            return self.output_func(sol, EnsembleContext(i))[0]
+            return self.output_func(sol, EnsembleContext(self.offset + i))[0]
         return sol
 
 
@@ -723,6 +731,22 @@ def solve(ens: EnsembleProblem, alg, ensemblealg: EnsembleGPUKernel, *, trajecto
         save_everystep = False if adaptive else True
     tstart = time.perf_counter()
     parts, t0s = [], []
+    if ens.reduction is not None:
+        # solve.jl:97-164: each batch is solved, turned into its solutions and folded into u
+        u = [] if ens.u_init is None else ens.u_init
+        converged = False
+        for b0 in range(0, trajectories, batch_size):
+            I = range(b0, min(trajectories, b0 + batch_size))
+            u0, p, tsp, sa = _build_batch(ens, I)
+            dp = DeviceProblems(prob.f, u0, p, tsp, Tt, dev, sa)
+            r = _solve_device(dp, alg, adaptive, dt=dt, saveat=saveat, save_everystep=save_everystep,
+                              abstol=abstol, reltol=reltol, traj_offset=b0, callback=callback, tstops=tstops, **kw)
+            torch.cuda.synchronize(dev)
+            ts_b = r.ts.cpu().numpy()
+            sols = _LazySolutions(ts_b, r.us.cpu().numpy(), np.asarray(tsp)[:, 0].astype(ts_b.dtype), alg,
+                                  ens.output_func, "ode", offset=b0)
+            u, converged = ens.reduction(u, [sols[j] for j in range(len(sols))], I)
+        return EnsembleSolution(u, time.perf_counter() - tstart, True)
     for b0 in range(0, trajectories, batch_size):
         I = range(b0, min(trajectories, b0 + batch_size))
         u0, p, tsp, sa = _build_batch(ens, I)

@@ -445,3 +445,29 @@ def test_invalid_arguments_raise(degpu_mod):
         degpu_mod.vectorized_asolve(probs, None, degpu_mod.GPUEM(), dt=0.1)
     with pytest.raises(degpu_mod.DegpuError):
         degpu_mod.api._solve_device(probs, degpu_mod.GPUTsit5(), True, dt=-1.0)
+
+
+def test_ensemble_reduction_batches(degpu_mod):
+    """test/reduction.jl on the kernel path: u' = 1.01 u from ra[i] * 0.5, output_func keeps
+    the final state, reduction sums batch by batch (batch_size 20 of 100) -- equal to the
+    sum of the unreduced solve, and to the exact 0.5 e^1.01 sum(ra)."""
+    rng = np.random.default_rng(100)
+    ra = rng.random(100)
+    src = """template <class T>
+__device__ __forceinline__ void degpu_f(T* du, const T* u, const float* p, T t) { du[0] = 1.01f * u[0]; }"""
+    f = degpu_mod.ODEFunction(src, 1, 0)
+    prob = degpu_mod.ODEProblem(f, np.array([0.5], np.float32), (0.0, 1.0), np.zeros(0, np.float32),
+                                time_type=np.float64)
+    prob_func = lambda pr, ctx: degpu_mod.remake(pr, u0=np.float32(ra[ctx["sim_id"]]) * pr.u0)
+    output_func = lambda sol, ctx: (sol.u[-1], False)
+    reduction = lambda u, batch, I: (u + sum(batch), False)
+    e1 = degpu_mod.EnsembleProblem(prob, prob_func=prob_func, output_func=output_func)
+    s1 = degpu_mod.solve(e1, degpu_mod.GPUTsit5(), degpu_mod.EnsembleGPUKernel(0), trajectories=100, batch_size=20,
+                         reltol=1e-8, abstol=1e-8)
+    e2 = degpu_mod.EnsembleProblem(prob, prob_func=prob_func, output_func=output_func, reduction=reduction,
+                                   u_init=np.zeros(1, np.float32))
+    s2 = degpu_mod.solve(e2, degpu_mod.GPUTsit5(), degpu_mod.EnsembleGPUKernel(0), trajectories=100, batch_size=20,
+                         reltol=1e-8, abstol=1e-8)
+    total = sum(s1.u[i] for i in range(100))
+    assert np.allclose(total, s2.u, rtol=1e-6)
+    assert np.allclose(s2.u, 0.5 * np.exp(1.01) * ra.astype(np.float32).sum(), rtol=1e-4)
