@@ -471,3 +471,45 @@ __device__ __forceinline__ void degpu_f(T* du, const T* u, const float* p, T t) 
     total = sum(s1.u[i] for i in range(100))
     assert np.allclose(total, s2.u, rtol=1e-6)
     assert np.allclose(s2.u, 0.5 * np.exp(1.01) * ra.astype(np.float32).sum(), rtol=1e-4)
+
+
+@pytest.mark.parametrize("alg", ["GPUTsit5", "GPUVern7", "GPUVern9", "GPURosenbrock23", "GPURodas4"])
+def test_lower_level_api_lorenz(degpu_mod, oracle_mod, alg):
+    """test/lower_level_api.jl: 10,000 Lorenz problems with rand(Float32, 3) .* p, analytic
+    Jacobian and time gradient, Float32 tspan (0, 10); make_prob_compatible -> adapt ->
+    vectorized_solve / vectorized_asolve (save_everystep=false, dt=0.1f0, the default
+    tolerances).  The reference only runs them; here every member must end finite in fast
+    mode, and parity mode must reproduce the oracle bit for bit."""
+    import torch
+    rng = np.random.default_rng(0)
+    B = 10_000
+    base = np.array([10.0, 28.0, 8 / 3.0], np.float32)
+    base_src = degpu_mod.ODEFunction.builtin("lorenz").source
+    jac_src = """
+__device__ __forceinline__ void degpu_jac(float* J, const float* u, const float* p, float t) {
+  J[0] = -p[0]; J[1] = p[1] - u[2]; J[2] = u[1];
+  J[3] = p[0];  J[4] = -1.0f;       J[5] = u[0];
+  J[6] = 0.0f;  J[7] = -u[0];       J[8] = -p[2];
+}
+__device__ __forceinline__ void degpu_tgrad(float* dT, const float* u, const float* p, float t) {
+  dT[0] = 0.0f; dT[1] = 0.0f; dT[2] = 0.0f;
+}
+"""
+    f = degpu_mod.ODEFunction(base_src + jac_src, 3, 3, jac=True, tgrad=True)  # lorenz_jac / lorenz_tgrad
+    prob = degpu_mod.ODEProblem(f, np.array([1, 0, 0], np.float32), (0.0, 10.0), base)
+    ps = (rng.random((B, 3)).astype(np.float32) * base).astype(np.float32)
+    probs = [degpu_mod.make_prob_compatible(degpu_mod.remake(prob, p=ps[i])) for i in range(B)]
+    gpu_probs = degpu_mod.adapt(0, probs)
+    a = getattr(degpu_mod, alg)()
+    oalg = {"GPUTsit5": "tsit5", "GPUVern7": "vern7", "GPUVern9": "vern9", "GPURosenbrock23": "rosenbrock23",
+            "GPURodas4": "rodas4"}[alg]
+    u0 = np.tile(np.array([1, 0, 0], np.float32), (B, 1))
+    for adaptive, fn in ((False, degpu_mod.vectorized_solve), (True, degpu_mod.vectorized_asolve)):
+        ts, us = fn(gpu_probs, prob, a, save_everystep=False, dt=0.1)  # fast mode: every member finite
+        assert torch.isfinite(us[:, 1]).all()
+        ts, us = fn(gpu_probs, prob, a, save_everystep=False, dt=0.1, mode="parity")
+        kw = dict(abstol=1e-6, reltol=1e-3) if adaptive else {}
+        ots, ous, _, _, _ = oracle_mod.solve("lorenz", oalg, u0, ps, [0.0, 10.0], adaptive=adaptive,
+                                             dt=float(np.float32(0.1)), L=2, jac="analytic", **kw)
+        assert_bit_equal(us.cpu().numpy(), ous, f"us ({'asolve' if adaptive else 'solve'})")
+        assert_bit_equal(ts.cpu().numpy(), ots, "ts")
