@@ -283,6 +283,29 @@ def extra_configs(args, dev, flush):
         out3[drv] = {"trajectories_per_s": B3 / (ms * 1e-3), "ms": ms, "fp32_tflops": fl / (ms * 1e-3) / 1e12,
                      "attempts_per_traj_mean": float((na + nr).mean()), "attempts_per_traj_max": int((na + nr).max())}
     out3["persistent_speedup"] = out3["persistent"]["trajectories_per_s"] / out3["naive"]["trajectories_per_s"]
+    # persistent driver visiting the trajectories longest-first, by a work model trained
+    # (untimed) on 262,144 fresh draws of the same distribution, with the span tEnd as input
+    if not args.no_learned:
+        from degpu import learned
+        rng_w = np.random.default_rng(33)
+        Bw = 1 << 18
+        pw = np.stack([np.full(Bw, 10.0), rng_w.uniform(0, 100, Bw), np.full(Bw, 8 / 3)], 1).astype(np.float32)
+        tw = np.stack([np.zeros(Bw), rng_w.uniform(1, 20, Bw)], 1)
+        wm3, winfo3 = learned.fit_work_model(f, np.tile(np.array([1, 0, 0], np.float32), (Bw, 1)), pw, tw, np.float64,
+                                             degpu.GPUTsit5(), reltol=1e-6, abstol=1e-8, epochs=8)
+
+        def run3o():
+            holder["r"] = degpu.api._solve_device(pr3, degpu.GPUTsit5(), True, dt=0.1, abstol=1e-8, reltol=1e-6,
+                                                  driver="persistent", work_model=wm3)
+        ms = time_solve(run3o, reps=2)
+        r = holder["r"]
+        na, nr = r.naccept.cpu().numpy(), r.nreject.cpu().numpy()
+        fl = flops.solve_flops("tsit5", 3, "lorenz", na, nr, nsaves=0)
+        out3["persistent_ordered"] = {"trajectories_per_s": B3 / (ms * 1e-3), "ms": ms,
+                                      "fp32_tflops": fl / (ms * 1e-3) / 1e12, "work_model": winfo3,
+                                      "includes": "work-model inference + ordering kernels"}
+        out3["ordered_speedup_vs_persistent"] = (out3["persistent_ordered"]["trajectories_per_s"]
+                                                 / out3["persistent"]["trajectories_per_s"])
     res[f"uneven_lorenz_{B3}"] = out3
 
     # the adaptive Lorenz ensemble with GPUVern9 (the headline tolerances; FP32 state, so
@@ -425,46 +448,68 @@ def gpu_arm(args):
     def plain_launch():
         _lib.check(_lib.lib().degpu_plan_launch(plan, sptr))
 
-    # ---------------- learned controller: trained on the plain solver's traces (untimed)
-    lrn = None
+    # ---------------- learned parts, trained on the plain solver's traces (untimed):
+    #   step model  -- per-trajectory dt0 and tolerance scale (learned controller);
+    #   work models -- predicted attempts of the plain / learned solve, turned into a
+    #                  longest-first visiting order for the persistent driver.
+    # Each learned arm is one captured graph of degpu_learned_asolve_ex: inference, ordering
+    # and the solve, all inside the timed region.
+    arms = {}
     if not args.no_learned:
         t_train = time.perf_counter()
         ut, pt = make_inputs(args.train_trajectories, WORKLOAD["seed"] + 1000 + rank)
-        model, tinfo = learned.fit_step_model(f, ut, pt, WORKLOAD["tspan"], np.float64, degpu.GPUTsit5(),
-                                              reltol=WORKLOAD["reltol"], abstol=WORKLOAD["abstol"], epochs=8)
-        t_train = time.perf_counter() - t_train
-        lo = outputs()
+        step_model, tinfo = learned.fit_step_model(f, ut, pt, WORKLOAD["tspan"], np.float64, degpu.GPUTsit5(),
+                                                   reltol=WORKLOAD["reltol"], abstol=WORKLOAD["abstol"], epochs=8)
+        t_step = time.perf_counter() - t_train
+        t_train = time.perf_counter()
+        wm_plain, winfo_p = learned.fit_work_model(f, ut, pt, WORKLOAD["tspan"], np.float64, degpu.GPUTsit5(),
+                                                   reltol=WORKLOAD["reltol"], abstol=WORKLOAD["abstol"], epochs=8)
+        wm_lrn, winfo_l = learned.fit_work_model(f, ut, pt, WORKLOAD["tspan"], np.float64, degpu.GPUTsit5(),
+                                                 reltol=WORKLOAD["reltol"], abstol=WORKLOAD["abstol"], epochs=8,
+                                                 step_model=step_model)
+        t_work = time.perf_counter() - t_train
+        train_rec = {"trajectories": args.train_trajectories, "step_model_seconds": t_step, **tinfo,
+                     "work_models_seconds": t_work, "work_model_plain": winfo_p, "work_model_learned": winfo_l}
         lopt = degpu.api._options(degpu.GPUTsit5(), np.float64, dt=WORKLOAD["dt"], abstol=WORKLOAD["abstol"],
                                   reltol=WORKLOAD["reltol"], saveat_dev=sa_dev.data_ptr(), nsaveat=L,
                                   driver="persistent", traj_offset=rank * B, block=block, chunk=chunk)
+        for name, sm, wm, nlaunch in (("plain_ordered", None, wm_plain, 5), ("learned", step_model, None, 2),
+                                      ("learned_ordered", step_model, wm_lrn, 6)):
+            out = outputs()
 
-        def learned_call(st):
-            _lib.check(_lib.lib().degpu_learned_asolve(f.handle(), model.h, ctypes.byref(pr), ctypes.byref(lopt),
-                                                       model.dt_range[0], model.dt_range[1], model.scale_range[1],
-                                                       ctypes.byref(lo["c"]), ctypes.c_void_p(st.cuda_stream)))
-        learned_call(stream)  # compiles / loads outside the capture
-        torch.cuda.synchronize(dev)
-        g = torch.cuda.CUDAGraph()
-        cap = torch.cuda.Stream(dev)
-        with torch.cuda.graph(g, stream=cap):
-            learned_call(cap)
-        lrn = dict(graph=g, out=lo, model=model, info=tinfo, train_s=t_train)
+            def call(st, sm=sm, wm=wm, out=out):
+                _lib.check(_lib.lib().degpu_learned_asolve_ex(
+                    f.handle(), None if sm is None else sm.h, None if wm is None else wm.h, ctypes.byref(pr),
+                    ctypes.byref(lopt), step_model.dt_range[0], step_model.dt_range[1], step_model.scale_range[1],
+                    ctypes.byref(out["c"]), ctypes.c_void_p(st.cuda_stream)))
+            call(stream)  # compiles / loads outside the capture
+            torch.cuda.synchronize(dev)
+            g = torch.cuda.CUDAGraph()
+            cap = torch.cuda.Stream(dev)
+            with torch.cuda.graph(g, stream=cap):
+                call(cap)
+            arms[name] = dict(graph=g, out=out, launches=nlaunch)
 
     for _ in range(args.warmup):
         plain_launch()
-        if lrn:
-            lrn["graph"].replay()
+        for a in arms.values():
+            a["graph"].replay()
     torch.cuda.synchronize(dev)
     if dist:
         dist.barrier()
     with ClockSampler(local) as clk:
         torch.cuda.synchronize(dev)
         clk.mark(True)
+        # NVTX range "timed": lets a profiler select the timed launches (ncu --nvtx
+        # --nvtx-include "timed/"); a no-op otherwise
+        torch.cuda.nvtx.range_push("timed")
         wall0 = time.perf_counter()
         t_plain = timed_steps(plain_launch, args.steps, stream, flush)
-        t_lrn = timed_steps(lambda: lrn["graph"].replay(), args.steps, stream, flush) if lrn else None
+        for a in arms.values():
+            a["times"] = timed_steps(lambda a=a: a["graph"].replay(), args.steps, stream, flush)
         torch.cuda.synchronize(dev)
         wall = time.perf_counter() - wall0
+        torch.cuda.nvtx.range_pop()
         clk.mark(False)
 
     def agg(times):
@@ -477,14 +522,13 @@ def gpu_arm(args):
 
     ms_plain = agg(t_plain)
     v_plain = B * world * args.steps / (ms_plain * 1e-3)
-    ms_lrn = agg(t_lrn) if lrn else None
-    v_lrn = B * world * args.steps / (ms_lrn * 1e-3) if lrn else None
+    for a in arms.values():
+        a["ms"] = agg(a["times"])
+        a["value"] = B * world * args.steps / (a["ms"] * 1e-3)
 
     na_h, nr_h, rc_h = po["na"].cpu().numpy(), po["nr"].cpu().numpy(), po["rc"].cpu().numpy()
     us_h = po["us"].cpu().numpy()
     fl = flops.solve_flops("tsit5", 3, "lorenz", na_h, nr_h, nsaves=B * L)
-    kern_ms = ms_plain / args.steps
-    achieved = fl / (kern_ms * 1e-3) / 1e12
 
     # ---------------- end to end through the C ABI with host buffers (plain controller)
     e2e = None
@@ -528,15 +572,22 @@ def gpu_arm(args):
     idx = np.arange(0, B, max(1, B // 2048))[:2048]
     oref = oracle_reference(u0, p, idx)
     err_plain = oracle_error(us_h[:, -1, :], idx, oref)
-    learned_rec = None
-    if lrn:
-        lna, lnr, lrc = lrn["out"]["na"].cpu().numpy(), lrn["out"]["nr"].cpu().numpy(), lrn["out"]["rc"].cpu().numpy()
-        err_l = oracle_error(lrn["out"]["us"].cpu().numpy()[:, -1, :], idx, oref)
-        learned_rec = {"value": v_lrn, "ms_per_step": ms_lrn / args.steps, "oracle_error": err_l,
-                       "attempts_per_traj": float((lna + lnr).mean()),
-                       "reject_frac": float(lnr.sum() / max(1, (lna + lnr).sum())),
-                       "retcodes_ok": bool((lrc == 1).all()), "speedup_vs_plain": v_lrn / v_plain,
-                       "train": {"trajectories": args.train_trajectories, "seconds": lrn["train_s"], **lrn["info"]}}
+    arm_recs = {}
+    for name, a in arms.items():
+        o = a["out"]
+        ana, anr, arc = o["na"].cpu().numpy(), o["nr"].cpu().numpy(), o["rc"].cpu().numpy()
+        aus = o["us"].cpu().numpy()
+        rec = {"value": a["value"], "ms_per_step": a["ms"] / args.steps,
+               "oracle_error": oracle_error(aus[:, -1, :], idx, oref),
+               "attempts_per_traj": float((ana + anr).mean()),
+               "reject_frac": float(anr.sum() / max(1, (ana + anr).sum())),
+               "retcodes_ok": bool((arc == 1).all()), "speedup_vs_plain": a["value"] / v_plain,
+               "kernels_per_step": a["launches"],
+               "flops_per_launch": flops.solve_flops("tsit5", 3, "lorenz", ana, anr, nsaves=B * L)}
+        if name == "plain_ordered":  # same controller in another visiting order: same bits
+            rec["bit_identical_to_plain"] = bool(np.array_equal(aus.view(np.uint32), us_h.view(np.uint32))
+                                                 and np.array_equal(ana, na_h) and np.array_equal(arc, rc_h))
+        arm_recs[name] = rec
 
     extras = None if args.no_extras else extra_configs(args, dev, flush)
 
@@ -556,35 +607,54 @@ def gpu_arm(args):
     # so its traffic grows in proportion to B.
     traffic = TRAFFIC_BYTES_PER_TRAJ * B
 
-    # headline: the learned controller when it holds the plain run's error level and the bar
-    use_learned = bool(learned_rec and learned_rec["retcodes_ok"]
-                       and learned_rec["oracle_error"]["p90"] <= max(err_plain["p90"] * 1.25, 0.0)
-                       and learned_rec["oracle_error"]["p90"] <= 1e-4 and v_lrn > v_plain)
-    value = v_lrn if use_learned else v_plain
+    # headline: the fastest arm that holds the plain run's error level (p90 within 25 %) and
+    # the 1e-4 bar with every trajectory successful; the plain arm otherwise
+    plain_rec = {"value": v_plain, "ms_per_step": ms_plain / args.steps, "oracle_error": err_plain,
+                 "attempts_per_traj": float((na_h + nr_h).mean()),
+                 "reject_frac": float(nr_h.sum() / max(1, (na_h + nr_h).sum())),
+                 "retcodes_ok": bool((rc_h == 1).all()), "kernels_per_step": 1, "flops_per_launch": fl}
+    best, best_rec = "plain", plain_rec
+    for name, rec in arm_recs.items():
+        ok = (rec["retcodes_ok"] and rec["oracle_error"]["p90"] <= max(err_plain["p90"] * 1.25, 0.0)
+              and rec["oracle_error"]["p90"] <= 1e-4)
+        rec["meets_error_rule"] = bool(ok)
+        if ok and rec["value"] > best_rec["value"]:
+            best, best_rec = name, rec
+    value = best_rec["value"]
+    method = {"plain": "plain PI controller, index order",
+              "plain_ordered": "plain PI controller, longest-first order from the learned work model (BF16 MLP)",
+              "learned": "learned dt0 + tolerance scale (BF16 MLP), index order",
+              "learned_ordered": "learned dt0 + tolerance scale and longest-first order (BF16 MLPs)"}[best]
+    # roofline of the headline run: its algorithmic flops (from its own attempt counters) over
+    # its event-timed step; a learned arm's step also holds the MLP inference and ordering
+    # kernels (tens of microseconds), charged to the solve
+    achieved = best_rec["flops_per_launch"] / (best_rec["ms_per_step"] * 1e-3) / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": (ms_lrn if use_learned else ms_plain) / args.steps,
+        "warmup": args.warmup, "ms_per_step": best_rec["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 state / f64 time",
         "data": "synthetic (seeded)",
-        "method": ("learned dt0 + tolerance scale (BF16 MLP), " if use_learned else "plain PI controller, ")
-        + "persistent warp-refill driver, CUDA graph",
+        "method": method + ", persistent warp-refill driver, CUDA graph",
         "config": {"workload": WORKLOAD["name"], "trajectories": B, "alg": "GPUTsit5 (adaptive)",
                    "reltol": WORKLOAD["reltol"], "abstol": WORKLOAD["abstol"], "saveat": "0:0.5:10",
                    "tspan": list(WORKLOAD["tspan"]), "l2": "flushed between timed steps (256 MiB memset)",
                    "parallelism": "one process per GPU, trajectories sharded" if world > 1 else "single GPU",
                    "block": block, "chunk": chunk, "grid": grid, "regs_per_thread": regs},
-        "plain": {"value": v_plain, "ms_per_step": ms_plain / args.steps, "oracle_error": err_plain,
-                  "attempts_per_traj": float((na_h + nr_h).mean()),
-                  "reject_frac": float(nr_h.sum() / max(1, (na_h + nr_h).sum())), "retcodes_ok": bool((rc_h == 1).all())},
-        "learned": learned_rec,
+        "headline_arm": best,
+        "plain": plain_rec,
+        "learned_arms": arm_recs or None,
+        "learned_training": train_rec if arms else None,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                     "frac": achieved / peak.value, "traffic": traffic, "kernel": "degpu_persistent_kernel (plain run)",
+                     "frac": achieved / peak.value, "traffic": traffic,
+                     "kernel": f"degpu_persistent_kernel ({best} run)",
                      "peak_source": "measured live: FP32 FMA probe (degpu_fp32_peak)",
-                     "flops_per_launch": fl, "attempts_per_traj": float((na_h + nr_h).mean())},
+                     "flops_per_launch": best_rec["flops_per_launch"],
+                     "attempts_per_traj": best_rec["attempts_per_traj"],
+                     "plain_index_order_frac": fl / (ms_plain / args.steps * 1e-3) / 1e12 / peak.value},
         "e2e": e2e,
         "cpu_baseline": cpu,
         "other_configs": extras,
-        "gpu_launches": args.steps * (3 if lrn else 1),
+        "gpu_launches": args.steps * (1 + sum(a["launches"] for a in arms.values())),
         "wall_s_timed_region": wall,
         "clocks": clk.summary(),
     }

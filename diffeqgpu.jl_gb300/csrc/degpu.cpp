@@ -517,6 +517,7 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   }
   P.ntstops = o->ntstops;
   P.tstops = o->ntstops ? o->tstops : nullptr;
+  P.order = k.driver == 2 ? o->order : nullptr;  // visiting order: persistent driver only
   k.tstops = o->ntstops > 0 ? 1 : 0;
   k.nccb = nc;
   k.ndcb = nd;
@@ -693,6 +694,7 @@ int degpu_batch_solve_host(const degpu_rhs* f, const float* u0, const float* p, 
                            signed char* retcode, int* naccept, int* nreject, void* stream) {
   if (!f || !opt) return fail(DEGPU_E_INVALID, "null argument");
   if (B < 0) return fail(DEGPU_E_INVALID, "negative trajectory count");
+  if (opt->order) return fail(DEGPU_E_INVALID, "the host-buffer API takes no visiting order (options.order)");
   if (B == 0) return 0;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t tsz = opt->time_type == DEGPU_TIME_F64 ? 8 : 4;
@@ -901,23 +903,49 @@ int degpu_kernel_info(const degpu_rhs* f, const degpu_options* opt, int adaptive
 
 int degpu_learned_asolve(const degpu_rhs* f, const degpu_mlp* m, const degpu_problems* probs, const degpu_options* opt,
                          float dt_lo, float dt_hi, float s_max, degpu_outputs* out, void* stream) {
-  if (!f || !m || !probs || !opt || !out) return fail(DEGPU_E_INVALID, "null argument");
+  if (!m) return fail(DEGPU_E_INVALID, "null argument");
+  return degpu_learned_asolve_ex(f, m, nullptr, probs, opt, dt_lo, dt_hi, s_max, out, stream);
+}
+
+int degpu_learned_asolve_ex(const degpu_rhs* f, const degpu_mlp* m, const degpu_mlp* work_model,
+                            const degpu_problems* probs, const degpu_options* opt, float dt_lo, float dt_hi,
+                            float s_max, degpu_outputs* out, void* stream) {
+  if (!f || !probs || !opt || !out) return fail(DEGPU_E_INVALID, "null argument");
   if (probs->B < 0) return fail(DEGPU_E_INVALID, "negative trajectory count");
   if (probs->B == 0) return 0;
-  if (!(s_max >= 1.0f) || !(dt_lo > 0.0f) || !(dt_hi >= dt_lo)) return fail(DEGPU_E_INVALID, "bad dt / scale clamp");
+  if (m && (!(s_max >= 1.0f) || !(dt_lo > 0.0f) || !(dt_hi >= dt_lo))) return fail(DEGPU_E_INVALID, "bad dt / scale clamp");
   cudaStream_t s = (cudaStream_t)stream;
-  float* scratch = nullptr;  // dt0 [B] followed by tolscale [B]
-  int rc = lib_alloc((void**)&scratch, sizeof(float) * 2 * (size_t)probs->B, s);
+  const size_t B = (size_t)probs->B;
+  // scratch: [dt0 | tolscale] (step model), [predicted work | unused | order] (work model)
+  const size_t n_step = m ? 2 * B : 0, n_work = work_model ? 3 * B : 0;
+  float* scratch = nullptr;
+  int rc = lib_alloc((void**)&scratch, sizeof(float) * (n_step + n_work), s);
   if (rc) return rc;
-  rc = degpu_mlp_infer_problems(m, probs->u0, f->N, probs->p, f->P, (float)opt->reltol, probs->B, scratch,
-                                    scratch + probs->B, dt_lo, dt_hi, 1.0f, s_max, stream);
-  if (rc) rc = fail(rc, "step-size model inference failed (does the model's input width match N + P + 1?)");
-  if (!rc) {
-    degpu_options o = *opt;
+  degpu_options o = *opt;
+  o.dt0 = nullptr;
+  o.tolscale = nullptr;
+  o.order = nullptr;
+  const int span_f64 = opt->time_type == DEGPU_TIME_F64;
+  if (m) {
+    rc = degpu_internal_mlp_infer_problems(m, probs->u0, f->N, probs->p, f->P, probs->tspan, span_f64,
+                                           (float)opt->reltol, probs->B, scratch, scratch + B, dt_lo, dt_hi, 1.0f,
+                                           s_max, stream);
+    if (rc) rc = fail(rc, "step-size model inference failed (input width must be N + P + 1, or N + P + 2 with the span)");
     o.dt0 = scratch;
-    o.tolscale = scratch + probs->B;
-    rc = degpu_vectorized_asolve(f, probs, &o, out, stream);
+    o.tolscale = scratch + B;
   }
+  if (!rc && work_model) {
+    // predicted attempts = exp(first output), clamped to [1, 2^31]; the second output is unused
+    float* work = scratch + n_step;
+    int* order = reinterpret_cast<int*>(scratch + n_step + 2 * B);
+    rc = degpu_internal_mlp_infer_problems(work_model, probs->u0, f->N, probs->p, f->P, probs->tspan, span_f64,
+                                           (float)opt->reltol, probs->B, work, nullptr, 1.0f, 2147483648.0f, 1.0f,
+                                           1.0f, stream);
+    if (rc) rc = fail(rc, "work model inference failed (input width must be N + P + 1, or N + P + 2 with the span)");
+    if (!rc) rc = degpu_work_order(work, probs->B, order, stream);
+    o.order = order;
+  }
+  if (!rc) rc = degpu_vectorized_asolve(f, probs, &o, out, stream);
   cudaFreeAsync(scratch, s);
   return rc;
 }
@@ -1069,6 +1097,8 @@ int degpu_internal_rhs_dims(const degpu_rhs* f, int* n_state, int* n_param) {
 }
 
 int degpu_internal_fail(int code, const char* msg) { return fail(code, msg ? msg : ""); }
+
+int degpu_internal_alloc(void** p, size_t n, void* stream) { return lib_alloc(p, n, (cudaStream_t)stream); }
 
 int degpu_internal_asolve_with_work(const degpu_rhs* f, const degpu_problems* probs, const degpu_options* opt,
                                     degpu_outputs* out, unsigned long long* work, void* stream) {

@@ -1888,9 +1888,15 @@ extern "C" __global__ void __launch_bounds__(DEGPU_LB_THREADS, DEGPU_LB_MINBLOCK
       }
       const int rank = __popc(idle & lt_mask);
       if (my < 0 && q_next + rank < q_end) {
-        my = q_next + rank;
-        lane_init(L, io, my);
-        if (!TP::lt(L.t, L.tf)) { lane_finish(L, io, my); fin = true; }
+        // work item -> trajectory: identity, or a caller-given visiting order (e.g. longest
+        // predicted work first, which shortens the tail where warps drain their last lanes)
+        const int w = q_next + rank;
+        const int tr = P.order ? __ldg(P.order + w) : w;
+        if ((unsigned)tr < (unsigned)B) {
+          my = tr;
+          lane_init(L, io, my);
+          if (!TP::lt(L.t, L.tf)) { lane_finish(L, io, my); fin = true; }
+        }
       }
       q_next = min(q_next + __popc(idle), q_end);
     }

@@ -59,6 +59,8 @@ typedef struct degpu_kparams {
   float ccb_nudge[8];
   float ccb_dtrelax[8];
   int dcb_fn[8];
+  const int* order;       /* persistent driver: work item w runs trajectory order[w] (null: w);
+                             entries outside [0, B) are skipped */
 } degpu_kparams;
 #define DEGPU_KP_MAX_CB 8
 

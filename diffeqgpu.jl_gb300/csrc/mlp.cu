@@ -4,13 +4,17 @@
 // dt and the same tolerances); the embedded error estimate still accepts or rejects every
 // step, so the plain controller remains the judge of every step.
 //
-// Numerics (the same in inference and training, quantisation-aware):
+// Numerics (the same rounding points in inference and training, quantisation-aware):
 //   xn = bf16((x - mean) / std);  z1 = W1q xn + b1;  h1 = bf16(silu(z1));
 //   z2 = W2q h1 + b2;  h2 = bf16(silu(z2));  y = W3q h2 + b3      (Wq = bf16(W), fp32 accumulate)
 // Inference runs on the tensor cores (mma.sync m16n8k16, bf16 in, fp32 accumulate: the
-// layers are 16-64 wide, far below a tcgen05 tile, and the whole network costs < 1 % of a
-// solve).  Training is FP32 SIMT: forward with the same bf16 rounding points, backward with
-// straight-through rounding, weight gradients as per-tile shared-memory GEMMs, Adam.
+// layers are 16-64 wide, far below a tcgen05 tile).  Its 128 activations per trajectory
+// would otherwise bound it on the special-function unit (a quarter of the FP32 rate): SiLU
+// there is z/2 + z/2 tanh(z/2) with the hardware tanh (one SFU op, relative error below
+// 2^-10, ahead of the bf16 rounding of h), ~0.07 ms per 10^6 trajectories.  Training is
+// FP32 SIMT with the exp/reciprocal logistic: forward with the same bf16 rounding points,
+// backward with straight-through rounding, weight gradients as per-tile shared-memory
+// GEMMs, Adam.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -21,6 +25,7 @@
 #include <vector>
 
 #include "degpu.h"
+#include "degpu_internal.h"
 
 namespace {
 
@@ -38,8 +43,19 @@ struct Layout {
 };
 
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
-__device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
+// logistic function with the SFU's exp2 and reciprocal (a few ulp; the hidden activations
+// are rounded to bf16 right after, and training and inference share this function).  For
+// z < -87 the denominator overflows and the quotient is 0, the limit.
+__device__ __forceinline__ float sigm(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float silu(float z) { return z * sigm(z); }
+// inference activation: z sigma(z) = h + h tanh(h), h = z/2, with tanh.approx.f32 (PTX ISA,
+// sm_75 and later)
+__device__ __forceinline__ float silu_fast(float z) {
+  const float h = 0.5f * z;
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+  return fmaf(h, t, h);
+}
 __device__ __forceinline__ float dsilu(float z) { float s = sigm(z); return s + z * s * (1.0f - s); }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -58,22 +74,30 @@ __device__ __forceinline__ void mma16816(float* d, const uint32_t* a, uint32_t b
 // ------------------------------------------------------------------ inference (tensor cores)
 // One warp per tile of 16 trajectories; weights staged once per CTA in shared memory as
 // bf16 [out][in] rows, which is exactly the "col" B-operand layout of mma.m16n8k16.
+// Rows are padded by 8 bf16 (16 bytes): a warp's B-fragment load reads row g = lane / 4,
+// column pair tig = lane % 4 of eight consecutive rows, and with unpadded 128-byte W2 rows
+// all eight rows start in the same bank (an 8-way conflict on every load); with 144-byte
+// (W2, W3) and 48-byte (W1) rows the 32 lanes hit 32 different banks.
+constexpr int WPAD = 8;
 struct InferSmem {
-  __nv_bfloat16 W1[H][KIN];
-  __nv_bfloat16 W2[H][H];
-  __nv_bfloat16 W3[8][H];  // rows >= NOUT are zero
+  __nv_bfloat16 W1[H][KIN + WPAD];
+  __nv_bfloat16 W2[H][H + WPAD];
+  __nv_bfloat16 W3[8][H + WPAD];  // rows >= NOUT are zero
   float b1[H], b2[H], b3[8];
   float mean[KIN], rstd[KIN];
 };
 
 // Features come either from x [B][n_in] or, when x is null, straight from the problem batch:
-// (u0 [B][Nu], p [B][Np], logtol), n_in = Nu + Np + 1.
+// (u0 [B][Nu], p [B][Np], logtol), n_in = Nu + Np + 1, optionally followed by the span
+// tf - t0 of the trajectory's tspan [B][2] (n_in = Nu + Np + 2; FP64 or FP32 tspan).
 struct FeatSrc {
   const float* x;
   const float* u0;
   const float* p;
   int Nu, Np;
   float logtol;
+  const void* tspan;
+  int tspan_f64;
 };
 
 __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* __restrict__ P, int n_in, const float* __restrict__ mean,
@@ -101,32 +125,52 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* __restrict_
   const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   const long long ntiles = (B + 15) / 16;
-  for (long long tile = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < ntiles; tile += warps) {
+  // raw feature k of row r (unnormalised); 0 outside the batch and the input width
+  auto raw = [&](long long r, int k) -> float {
+    if (r >= B || k >= n_in) return 0.0f;
+    if (src.x) return src.x[r * n_in + k];
+    if (k < src.Nu) return src.u0[r * src.Nu + k];
+    if (k < src.Nu + src.Np) return src.p[r * src.Np + (k - src.Nu)];
+    if (k == src.Nu + src.Np) return src.logtol;
+    if (src.tspan_f64) return (float)(((const double*)src.tspan)[2 * r + 1] - ((const double*)src.tspan)[2 * r]);
+    return ((const float*)src.tspan)[2 * r + 1] - ((const float*)src.tspan)[2 * r];
+  };
+  // this lane's 8 A-fragment features of a tile: rows g and g + 8, columns 2 tig + {0, 1, 8, 9}
+  auto load_tile = [&](long long tile, float* f) {
     const long long r0 = tile * 16 + g, r1 = r0 + 8;
-    auto feat = [&](long long r, int k) -> float {
-      if (r >= B || k >= n_in) return 0.0f;
-      float v;
-      if (src.x) v = src.x[r * n_in + k];
-      else if (k < src.Nu) v = src.u0[r * src.Nu + k];
-      else if (k < src.Nu + src.Np) v = src.p[r * src.Np + (k - src.Nu)];
-      else v = src.logtol;
-      return (v - S.mean[k]) * S.rstd[k];
-    };
+    f[0] = raw(r0, tig * 2); f[1] = raw(r0, tig * 2 + 1); f[2] = raw(r1, tig * 2); f[3] = raw(r1, tig * 2 + 1);
+    f[4] = raw(r0, tig * 2 + 8); f[5] = raw(r0, tig * 2 + 9); f[6] = raw(r1, tig * 2 + 8); f[7] = raw(r1, tig * 2 + 9);
+  };
+  const int c0 = tig * 2, c1 = tig * 2 + 1, c8 = tig * 2 + 8, c9 = tig * 2 + 9;
+  const float m0 = S.mean[c0], m1 = S.mean[c1], m8 = S.mean[c8], m9 = S.mean[c9];
+  const float s0 = S.rstd[c0], s1 = S.rstd[c1], s8 = S.rstd[c8], s9 = S.rstd[c9];
+  long long tile = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  float fnext[8];
+  if (tile < ntiles) load_tile(tile, fnext);
+  for (; tile < ntiles; tile += warps) {
+    const long long r0 = tile * 16 + g, r1 = r0 + 8;
+    // the next tile's features are loaded before this tile's layers run (their global-memory
+    // latency overlaps the tensor-core and activation work)
+    float f[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) f[j] = fnext[j];
+    if (tile + warps < ntiles) load_tile(tile + warps, fnext);
     uint32_t a[4];
-    a[0] = pack_bf16(feat(r0, tig * 2), feat(r0, tig * 2 + 1));
-    a[1] = pack_bf16(feat(r1, tig * 2), feat(r1, tig * 2 + 1));
-    a[2] = pack_bf16(feat(r0, tig * 2 + 8), feat(r0, tig * 2 + 9));
-    a[3] = pack_bf16(feat(r1, tig * 2 + 8), feat(r1, tig * 2 + 9));
+    a[0] = pack_bf16((f[0] - m0) * s0, (f[1] - m1) * s1);
+    a[1] = pack_bf16((f[2] - m0) * s0, (f[3] - m1) * s1);
+    a[2] = pack_bf16((f[4] - m8) * s8, (f[5] - m9) * s9);
+    a[3] = pack_bf16((f[6] - m8) * s8, (f[7] - m9) * s9);
     // layer 1: 8 n-tiles of 8 outputs
     float h[8][4];
 #pragma unroll
     for (int nt = 0; nt < 8; nt++) {
-      h[nt][0] = h[nt][1] = h[nt][2] = h[nt][3] = 0.0f;
+      // the accumulator starts at the bias (z = b + W x, the training kernel's order)
+      const float bb0 = S.b1[nt * 8 + tig * 2], bb1 = S.b1[nt * 8 + tig * 2 + 1];
+      h[nt][0] = bb0; h[nt][1] = bb1; h[nt][2] = bb0; h[nt][3] = bb1;
       const __nv_bfloat16* w = &S.W1[nt * 8 + g][0];
       mma16816(h[nt], a, *reinterpret_cast<const uint32_t*>(w + tig * 2), *reinterpret_cast<const uint32_t*>(w + tig * 2 + 8));
-      const float bb0 = S.b1[nt * 8 + tig * 2], bb1 = S.b1[nt * 8 + tig * 2 + 1];
-      h[nt][0] = silu(h[nt][0] + bb0); h[nt][1] = silu(h[nt][1] + bb1);
-      h[nt][2] = silu(h[nt][2] + bb0); h[nt][3] = silu(h[nt][3] + bb1);
+      h[nt][0] = silu_fast(h[nt][0]); h[nt][1] = silu_fast(h[nt][1]);
+      h[nt][2] = silu_fast(h[nt][2]); h[nt][3] = silu_fast(h[nt][3]);
     }
     // layer 2: accumulator fragments of layer 1 become the A fragments (k-tile kt = n-tiles 2kt, 2kt+1)
     uint32_t ha[4][4];
@@ -140,17 +184,17 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* __restrict_
     float h2[8][4];
 #pragma unroll
     for (int nt = 0; nt < 8; nt++) {
-      h2[nt][0] = h2[nt][1] = h2[nt][2] = h2[nt][3] = 0.0f;
+      const float bb0 = S.b2[nt * 8 + tig * 2], bb1 = S.b2[nt * 8 + tig * 2 + 1];
+      h2[nt][0] = bb0; h2[nt][1] = bb1; h2[nt][2] = bb0; h2[nt][3] = bb1;
       const __nv_bfloat16* w = &S.W2[nt * 8 + g][0];
 #pragma unroll
       for (int kt = 0; kt < 4; kt++)
         mma16816(h2[nt], ha[kt], *reinterpret_cast<const uint32_t*>(w + kt * 16 + tig * 2),
                  *reinterpret_cast<const uint32_t*>(w + kt * 16 + tig * 2 + 8));
-      const float bb0 = S.b2[nt * 8 + tig * 2], bb1 = S.b2[nt * 8 + tig * 2 + 1];
-      h2[nt][0] = silu(h2[nt][0] + bb0); h2[nt][1] = silu(h2[nt][1] + bb1);
-      h2[nt][2] = silu(h2[nt][2] + bb0); h2[nt][3] = silu(h2[nt][3] + bb1);
+      h2[nt][0] = silu_fast(h2[nt][0]); h2[nt][1] = silu_fast(h2[nt][1]);
+      h2[nt][2] = silu_fast(h2[nt][2]); h2[nt][3] = silu_fast(h2[nt][3]);
     }
-    float o[4] = {0.f, 0.f, 0.f, 0.f};
+    float o[4] = {S.b3[tig * 2], S.b3[tig * 2 + 1], S.b3[tig * 2], S.b3[tig * 2 + 1]};
 #pragma unroll
     for (int kt = 0; kt < 4; kt++) {
       uint32_t a2[4] = {pack_bf16(h2[2 * kt][0], h2[2 * kt][1]), pack_bf16(h2[2 * kt][2], h2[2 * kt][3]),
@@ -160,7 +204,7 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* __restrict_
                *reinterpret_cast<const uint32_t*>(w + kt * 16 + tig * 2 + 8));
     }
     if (tig == 0) {  // columns 0 and 1 live in lanes with tig == 0
-      const float y00 = o[0] + S.b3[0], y01 = o[1] + S.b3[1], y10 = o[2] + S.b3[0], y11 = o[3] + S.b3[1];
+      const float y00 = o[0], y01 = o[1], y10 = o[2], y11 = o[3];
       if (r0 < B) {
         if (y) { y[r0 * 2] = y00; y[r0 * 2 + 1] = y01; }
         if (dt0) dt0[r0] = fminf(fmaxf(__expf(y00), dt_lo), dt_hi);
@@ -394,6 +438,18 @@ int degpu_mlp_get_params(const degpu_mlp* m, float* host_params, float* host_gra
   return 0;
 }
 
+// resident inference blocks per SM: one wave of blocks, each staging the weights once and
+// striding over the 16-trajectory tiles
+static int infer_blocks_per_sm() {
+  static int n = 0;
+  if (!n) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, mlp_infer_kernel, 128, 0) != cudaSuccess || b < 1) b = 1;
+    n = b;
+  }
+  return n;
+}
+
 int degpu_mlp_infer(const degpu_mlp* m, const float* x, long long B, float* y, float* dt0, float* tolscale,
                     float dt_lo, float dt_hi, float s_lo, float s_hi, void* stream) {
   if (!m || B < 0 || (B > 0 && !x)) return DEGPU_E_INVALID;
@@ -402,8 +458,8 @@ int degpu_mlp_infer(const degpu_mlp* m, const float* x, long long B, float* y, f
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   long long tiles = (B + 15) / 16;
-  long long grid = std::min<long long>((tiles + 3) / 4, (long long)sms * 8);
-  FeatSrc src{x, nullptr, nullptr, 0, 0, 0.0f};
+  long long grid = std::min<long long>((tiles + 3) / 4, (long long)sms * infer_blocks_per_sm());
+  FeatSrc src{x, nullptr, nullptr, 0, 0, 0.0f, nullptr, 0};
   mlp_infer_kernel<<<(int)grid, 128, 0, (cudaStream_t)stream>>>(m->P, m->n_in, m->mean, m->stdv, src, B, y, dt0, tolscale,
                                                                  dt_lo, dt_hi, s_lo, s_hi);
   return cudaGetLastError() == cudaSuccess ? 0 : DEGPU_E_CUDA;
@@ -412,18 +468,8 @@ int degpu_mlp_infer(const degpu_mlp* m, const float* x, long long B, float* y, f
 int degpu_mlp_infer_problems(const degpu_mlp* m, const float* u0, int n_state, const float* p, int n_param, float reltol,
                              long long B, float* dt0, float* tolscale, float dt_lo, float dt_hi, float s_lo, float s_hi,
                              void* stream) {
-  if (!m || B < 0 || n_state + n_param + 1 != m->n_in || !(reltol > 0.0f)) return DEGPU_E_INVALID;
-  if (B == 0) return 0;
-  if (!u0 || (n_param > 0 && !p)) return DEGPU_E_INVALID;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  long long tiles = (B + 15) / 16;
-  long long grid = std::min<long long>((tiles + 3) / 4, (long long)sms * 8);
-  FeatSrc src{nullptr, u0, p, n_state, n_param, log10f(reltol)};
-  mlp_infer_kernel<<<(int)grid, 128, 0, (cudaStream_t)stream>>>(m->P, m->n_in, m->mean, m->stdv, src, B, nullptr, dt0,
-                                                                 tolscale, dt_lo, dt_hi, s_lo, s_hi);
-  return cudaGetLastError() == cudaSuccess ? 0 : DEGPU_E_CUDA;
+  return degpu_internal_mlp_infer_problems(m, u0, n_state, p, n_param, nullptr, 0, reltol, B, dt0, tolscale, dt_lo, dt_hi,
+                                           s_lo, s_hi, stream);
 }
 
 int degpu_mlp_grad(degpu_mlp* m, const float* x, const float* target, const float* weight, long long B, float* loss_out,
@@ -460,3 +506,22 @@ int degpu_mlp_adam_step(degpu_mlp* m, float lr, float beta1, float beta2, float 
 }
 
 }  // extern "C"
+
+int degpu_internal_mlp_infer_problems(const degpu_mlp* m, const float* u0, int n_state, const float* p, int n_param,
+                                      const void* tspan, int tspan_f64, float reltol, long long B, float* dt0,
+                                      float* tolscale, float dt_lo, float dt_hi, float s_lo, float s_hi, void* stream) {
+  if (!m || B < 0 || !(reltol > 0.0f)) return DEGPU_E_INVALID;
+  const int base = n_state + n_param + 1;
+  if (m->n_in != base && !(m->n_in == base + 1 && tspan)) return DEGPU_E_INVALID;
+  if (B == 0) return 0;
+  if (!u0 || (n_param > 0 && !p)) return DEGPU_E_INVALID;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long tiles = (B + 15) / 16;
+  long long grid = std::min<long long>((tiles + 3) / 4, (long long)sms * infer_blocks_per_sm());
+  FeatSrc src{nullptr, u0, p, n_state, n_param, log10f(reltol), m->n_in == base + 1 ? tspan : nullptr, tspan_f64};
+  mlp_infer_kernel<<<(int)grid, 128, 0, (cudaStream_t)stream>>>(m->P, m->n_in, m->mean, m->stdv, src, B, nullptr, dt0,
+                                                                 tolscale, dt_lo, dt_hi, s_lo, s_hi);
+  return cudaGetLastError() == cudaSuccess ? 0 : DEGPU_E_CUDA;
+}

@@ -84,5 +84,6 @@ extern "C" int degpu_learned_asolve_noalloc(const degpu_rhs* f, const degpu_mlp*
   degpu_options o = *opt;
   o.dt0 = dt0;
   o.tolscale = tolscale;
+  o.order = nullptr;  // ignored, as in degpu_learned_asolve
   return degpu_internal_asolve_with_work(f, probs, &o, out, work, stream);
 }

@@ -32,6 +32,7 @@ class Options(ctypes.Structure):
         ("dt0", ctypes.c_void_p), ("tolscale", ctypes.c_void_p), ("seed", ctypes.c_ulonglong),
         ("traj_offset", ctypes.c_longlong), ("block", ctypes.c_int), ("chunk", ctypes.c_int),
         ("ntstops", ctypes.c_int), ("tstops", ctypes.c_void_p), ("callbacks", ctypes.c_void_p),
+        ("order", ctypes.c_void_p),
     ]
 
 
@@ -102,6 +103,10 @@ SIGNATURES = {
                                                 ctypes.c_float, ctypes.c_float, _P]),
     "degpu_learned_asolve": (ctypes.c_int, [_P, _P, ctypes.POINTER(Problems), ctypes.POINTER(Options), ctypes.c_float,
                                             ctypes.c_float, ctypes.c_float, ctypes.POINTER(Outputs), _P]),
+    "degpu_learned_asolve_ex": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(Problems), ctypes.POINTER(Options),
+                                               ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                               ctypes.POINTER(Outputs), _P]),
+    "degpu_work_order": (ctypes.c_int, [_P, ctypes.c_longlong, _P, _P]),
     "degpu_learned_asolve_noalloc": (ctypes.c_int, [_P, _P, ctypes.POINTER(Problems), ctypes.POINTER(Options),
                                                     ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                                     ctypes.POINTER(Outputs), _P]),

@@ -486,7 +486,8 @@ def _torch_device(dev):
 
 def _options(alg, Tt, *, dt, abstol=1e-6, reltol=1e-3, save_everystep=False, saveat_dev=None, nsaveat=0,
              per_traj=False, mode="fast", driver="auto", maxiters=0, dt0=None, tolscale=None, seed=0,
-             traj_offset=0, block=0, chunk=0, jac="auto", tstops_dev=None, ntstops=0, callbacks_ptr=None):
+             traj_offset=0, block=0, chunk=0, jac="auto", tstops_dev=None, ntstops=0, callbacks_ptr=None,
+             order=None):
     o = _lib.Options()
     o.alg = alg.alg_id
     o.time_type = _lib.TIME_F64 if Tt == np.float64 else _lib.TIME_F32
@@ -513,6 +514,7 @@ def _options(alg, Tt, *, dt, abstol=1e-6, reltol=1e-3, save_everystep=False, sav
     o.ntstops = int(ntstops)
     o.tstops = tstops_dev
     o.callbacks = callbacks_ptr
+    o.order = order
     return o
 
 
@@ -570,6 +572,9 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
     dtf = torch.zeros(B, dtype=torch.float32, device=dev) if trace else None
     dt0 = kw.pop("dt0", None)
     tolscale = kw.pop("tolscale", None)
+    order = kw.pop("order", None)
+    step_model = kw.pop("step_model", None)  # learned controller (degpu.learned.StepSizeModel)
+    work_model = kw.pop("work_model", None)  # learned visiting order (degpu.learned.fit_work_model)
     ts_dev = None
     if tstops is not None and np.size(tstops):
         ts_dev = torch.as_tensor(np.sort(np.asarray(tstops, dtype=Tt).ravel()), device=dev)
@@ -582,6 +587,7 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
                    nsaveat=0 if sa_dev is None else L, per_traj=per_traj,
                    dt0=None if dt0 is None else dt0.data_ptr(),
                    tolscale=None if tolscale is None else tolscale.data_ptr(),
+                   order=None if order is None else order.data_ptr(),
                    tstops_dev=None if ts_dev is None else ts_dev.data_ptr(),
                    ntstops=0 if ts_dev is None else ts_dev.numel(),
                    callbacks_ptr=None if cb_struct is None else ctypes.addressof(cb_struct), **kw)
@@ -590,6 +596,16 @@ def _solve_device(probs: DeviceProblems, alg, adaptive: bool, *, dt, saveat=None
     st = stream if stream is not None else torch.cuda.current_stream(dev)
     pr = probs.cstruct()
     with torch.cuda.device(dev):
+        if step_model is not None or work_model is not None:
+            if not adaptive or isinstance(alg, GPUSDEAlgorithm):
+                raise ValueError("step and work models apply to adaptive ODE solves")
+            lo, hi = step_model.dt_range if step_model is not None else (1e-8, 1e3)
+            smax = step_model.scale_range[1] if step_model is not None else 1.0
+            check(lib().degpu_learned_asolve_ex(f.handle(), None if step_model is None else step_model.h,
+                                                None if work_model is None else work_model.h, ctypes.byref(pr),
+                                                ctypes.byref(opt), lo, hi, smax, ctypes.byref(out),
+                                                ctypes.c_void_p(st.cuda_stream)))
+            return KernelResult(ts, us, rc, na, nr, dtf)
         if isinstance(alg, GPUSDEAlgorithm):
             fn = lib().degpu_vectorized_solve_sde
         elif adaptive:

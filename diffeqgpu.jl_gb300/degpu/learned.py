@@ -2,6 +2,12 @@
 scale from (u0, p, log10 reltol), trained on the GPU by libdegpu's own kernels on traces
 that the plain solver generates.  No counterpart in the reference.
 
+A second network of the same shape, the work model, predicts each trajectory's step
+attempts (first output, log scale) from the same features; degpu_work_order turns the
+predictions into a longest-first visiting order for the persistent driver, which shortens
+the drain at the end of an ensemble with uneven step counts.  Results do not depend on the
+order; only the schedule does.
+
 Targets, from two plain solves of the training ensemble (both on the GPU):
   * log dt0    -- the first step the plain controller accepted (accepted-step trace);
   * log scale  -- how far the trajectory's tolerances can be relaxed before its final-state
@@ -20,7 +26,8 @@ import numpy as np
 from . import _lib
 from ._lib import check, lib
 
-N_OUT = 2
+N_OUT = 2     # DEGPU_MLP_OUT
+HIDDEN = 64   # DEGPU_MLP_HIDDEN
 
 
 def _sigs():
@@ -28,12 +35,16 @@ def _sigs():
     lib()
 
 
-def features(u0, p, reltol):
-    """x = (u0, p, log10 reltol) per trajectory, float32 [B, N + P + 1]."""
+def features(u0, p, reltol, span=None):
+    """x = (u0, p, log10 reltol) per trajectory, float32 [B, N + P + 1], followed by the
+    span tf - t0 of each trajectory's tspan when given ([B, N + P + 2])."""
     u0 = np.asarray(u0, np.float32)
     p = np.asarray(p, np.float32).reshape(u0.shape[0], -1)
     lt = np.broadcast_to(np.log10(np.asarray(reltol, np.float64)), (u0.shape[0],)).astype(np.float32)
-    return np.concatenate([u0, p, lt[:, None]], axis=1).astype(np.float32)
+    cols = [u0, p, lt[:, None]]
+    if span is not None:
+        cols.append(np.broadcast_to(np.asarray(span, np.float64), (u0.shape[0],)).astype(np.float32)[:, None])
+    return np.concatenate(cols, axis=1).astype(np.float32)
 
 
 class StepSizeModel:
@@ -119,8 +130,15 @@ class StepSizeModel:
         return y if raw else (d0, sc)
 
     # -------------------------------------------------------------- training
-    def fit(self, x, targets, weights=None, *, epochs=8, batch=8192, lr=3e-3, seed=0, log=None):
-        """Adam on the weighted MSE; x, targets, weights are host arrays or device tensors."""
+    def fit(self, x, targets, weights=None, *, epochs=8, batch=8192, lr=3e-3, seed=0, log=None,
+            normalize_targets=True):
+        """Adam on the weighted MSE; x, targets, weights are host arrays or device tensors.
+
+        With normalize_targets, each output is trained on its target standardised over the
+        samples that weight it, and the output layer is rescaled afterwards (W3 row * std,
+        b3 * std + mean), so the network predicts the targets in their own units: Adam moves
+        each weight by about lr per step, and an output offset of several units (log step
+        attempts ~ 5) would otherwise take thousands of steps to reach."""
         import torch
         dev = torch.device("cuda", torch.cuda.current_device())
         x = torch.as_tensor(np.asarray(x, np.float32) if not torch.is_tensor(x) else x, device=dev)
@@ -130,6 +148,16 @@ class StepSizeModel:
         mean = x.mean(0).cpu().numpy()
         std = x.std(0).clamp_min(1e-6).cpu().numpy()
         self.set(mean=mean, std=std)
+        t_mu = np.zeros(N_OUT)
+        t_sd = np.ones(N_OUT)
+        if normalize_targets:
+            td = t.double()
+            for o in range(N_OUT):
+                sel = td[:, o] if w is None else td[:, o][w[:, o] > 0]
+                if sel.numel() > 1:
+                    t_mu[o] = float(sel.mean())
+                    t_sd[o] = max(float(sel.std()), 1e-6)
+            t = ((td - torch.as_tensor(t_mu, device=dev)) / torch.as_tensor(t_sd, device=dev)).float().contiguous()
         n = x.shape[0]
         g = torch.Generator(device=dev)
         g.manual_seed(seed)
@@ -152,6 +180,15 @@ class StepSizeModel:
             hist.append(float(tot) / n)
             if log:
                 log(f"epoch {ep}: loss {hist[-1]:.5f}")
+        if normalize_targets:
+            p, _, mu, sd = self.get()
+            o_b3 = self.count - N_OUT
+            o_W3 = o_b3 - N_OUT * HIDDEN
+            W3 = p[o_W3:o_b3].reshape(N_OUT, HIDDEN).astype(np.float64)
+            b3 = p[o_b3:].astype(np.float64)
+            p[o_W3:o_b3] = (W3 * t_sd[:, None]).ravel().astype(np.float32)
+            p[o_b3:] = (b3 * t_sd + t_mu).astype(np.float32)
+            self.set(p, mu, sd)
         return hist
 
 
@@ -263,4 +300,68 @@ def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_qu
         m.shift_log_scale(shift)
         info.update({"calib_trajectories": nc, "calib_log_scale_shift": shift, "calib_q_plain": q_plain,
                      "calib_q_learned": q if shift < 50.0 else None})
+    return m, info
+
+
+# ---------------------------------------------------------------------- work model
+def work_order(work, stream=None):
+    """Longest-first visiting order (device int32 [B]) from a per-trajectory work estimate
+    (device float32 [B], e.g. predicted attempts), by degpu_work_order."""
+    import torch
+    st = stream or torch.cuda.current_stream(work.device)
+    work = work.contiguous().float()
+    order = torch.empty(work.shape[0], dtype=torch.int32, device=work.device)
+    check(lib().degpu_work_order(work.data_ptr(), work.shape[0], order.data_ptr(), ctypes.c_void_p(st.cuda_stream)))
+    return order
+
+
+def predicted_work(model, u0_dev, p_dev, reltol):
+    """Predicted step attempts (device float32 [B]) of a work model on device (u0, p)."""
+    import torch
+    B = u0_dev.shape[0]
+    x = torch.cat([u0_dev.float(), p_dev.float().reshape(B, -1),
+                   torch.full((B, 1), float(np.log10(reltol)), dtype=torch.float32, device=u0_dev.device)], 1)
+    y = model.infer(x.contiguous(), raw=True)
+    return torch.exp(y[:, 0]).clamp(1.0, 2.0 ** 31)
+
+
+def fit_work_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, dt=0.1, step_model=None, epochs=8, seed=0,
+                   holdout_frac=0.125, log=None, **solve_kw):
+    """Train a work model on the step attempts of the solve it will order.
+
+    The training solve is the plain controller, or the learned one when `step_model` is
+    given (its dt0 / tolerance-scale predictions change the attempts).  Targets are
+    log(naccept + nreject) of successful trajectories; the second output is unused (weight
+    0).  With per-trajectory tspans ([B, 2]) the span tf - t0 is an input too.  Returns
+    (model, info) with the correlation of predicted and actual log attempts on a held-out
+    share of the ensemble."""
+    import torch
+
+    from .api import DeviceProblems, _solve_device
+    dev = torch.device("cuda", torch.cuda.current_device())
+    B = u0.shape[0]
+    per_traj = np.ndim(tspan) == 2
+    tsp = np.asarray(tspan) if per_traj else np.broadcast_to(np.asarray(tspan, dtype=time_type), (B, 2))
+    probs = DeviceProblems(f, u0, p, tsp, time_type, dev)
+    span = (tsp[:, 1].astype(np.float64) - tsp[:, 0]) if per_traj else None
+    x = features(u0, p, np.full(B, reltol), span)
+    kw = {}
+    if step_model is not None:
+        d0, sc = step_model.infer(torch.as_tensor(x, device=dev))
+        kw = dict(dt0=d0.contiguous(), tolscale=sc.contiguous())
+    r = _solve_device(probs, alg, True, dt=dt, abstol=abstol, reltol=reltol, **kw, **solve_kw)
+    work = (r.naccept + r.nreject).cpu().numpy().astype(np.float64)
+    ok = (r.retcode.cpu().numpy() == 1) & (work > 0)
+    y = np.stack([np.log(np.maximum(work, 1.0)), np.zeros(B)], 1).astype(np.float32)
+    w = np.stack([ok, np.zeros(B, bool)], 1).astype(np.float32)
+    nh = int(B * holdout_frac)
+    m = StepSizeModel(x.shape[1], seed=seed)
+    m.dt_range = (1.0, 2.0 ** 31)  # exp(first output) = predicted attempts
+    m.scale_range = (1.0, 1.0)
+    m.fit(x[nh:], y[nh:], w[nh:], epochs=epochs, batch=2048, seed=seed, log=log)
+    info = {"n_train": int(B - nh), "attempts_mean": float(work[ok].mean()) if ok.any() else None}
+    if nh > 0:
+        yh = m.infer(torch.as_tensor(x[:nh], device=dev), raw=True)[:, 0].cpu().numpy()
+        sel = ok[:nh]
+        info["holdout_corr_log_attempts"] = float(np.corrcoef(yh[sel], y[:nh, 0][sel])[0, 1]) if sel.sum() > 2 else None
     return m, info

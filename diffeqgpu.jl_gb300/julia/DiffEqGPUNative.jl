@@ -45,6 +45,7 @@ Base.@kwdef mutable struct Options
     ntstops::Cint = 0
     tstops::Ptr{Cvoid} = C_NULL          # CuArray of the time type (the `tstops` kwarg)
     callbacks::Ptr{Cvoid} = C_NULL       # Ref{Callbacks}, see below
+    order::Ptr{Cint} = C_NULL            # optional CuArray{Cint} visiting order (degpu_work_order)
 end
 
 # GPUContinuousCallback fields the kernels use (callbacks.jl:34-124); the condition and

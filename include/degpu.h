@@ -138,6 +138,11 @@ typedef struct degpu_options {
   int ntstops;          /* tstops: 0 = none */
   const void* tstops;   /* device [ntstops] of the time type, ascending, shared by all trajectories */
   const degpu_callbacks* callbacks; /* NULL = no callbacks (CallbackSet(nothing)) */
+  const int* order;     /* optional device [B]: the persistent driver (the default adaptive
+                           driver) visits trajectory order[w] as its w-th work item, e.g. the
+                           permutation of degpu_work_order; results are the same in any order.
+                           Entries outside [0, B) are skipped.  Other drivers, and the
+                           host-buffer API (which rejects it), run trajectories in index order. */
 } degpu_options;
 
 /* outputs (caller-owned device buffers) */
@@ -275,6 +280,25 @@ int degpu_learned_asolve(const degpu_rhs* f, const degpu_mlp* m, const degpu_pro
 int degpu_learned_asolve_noalloc(const degpu_rhs* f, const degpu_mlp* m, const degpu_problems* probs,
                                  const degpu_options* opt, float dt_lo, float dt_hi, float s_max, degpu_outputs* out,
                                  void* stream);
+/* Visiting order for the persistent driver from a per-trajectory work estimate (device
+ * work [B], e.g. predicted step attempts): order [B] (device) lists the trajectories by
+ * descending work in quarter-octave classes of the estimate (floor(4 log2 work), clamped
+ * to 0..127; NaN and work < 1 fall in class 0), in unspecified order inside a class.
+ * Longest-first visiting shortens the tail of an ensemble with uneven step counts, where
+ * each warp drains its last lanes one by one.  Scratch: 1 KB from the stream-ordered
+ * allocator.  No counterpart in the reference. */
+int degpu_work_order(const float* work, long long B, int* order, void* stream);
+/* degpu_learned_asolve with optional parts: `m` (may be NULL: plain controller) predicts
+ * dt0 and the tolerance scale as above; `work_model` (may be NULL: index order) is a
+ * degpu_mlp whose first output is the predicted log step attempts of this solve, turned
+ * into a visiting order by degpu_work_order.  Either model may take one more input after
+ * log10 reltol, the span tf - t0 of each trajectory's tspan (input width N + P + 2), for
+ * ensembles with per-trajectory tspans.  Scratch: 8 bytes per trajectory per model, plus 4
+ * for the order, from the stream-ordered allocator.  opt->dt0 / tolscale / order are
+ * ignored. */
+int degpu_learned_asolve_ex(const degpu_rhs* f, const degpu_mlp* m, const degpu_mlp* work_model,
+                            const degpu_problems* probs, const degpu_options* opt, float dt_lo, float dt_hi,
+                            float s_max, degpu_outputs* out, void* stream);
 /* Gradient of the weighted mean squared error over a device batch (target, weight [B][2];
  * weight may be NULL) into the model's gradient buffer; *loss (device scalar, optional). */
 int degpu_mlp_grad(degpu_mlp* m, const float* x, const float* target, const float* weight, long long B, float* loss,

@@ -172,6 +172,33 @@ def test_argument_validation_without_gpu(degpu_mod):
     assert degpu_mod.lib().degpu_rhs_create(b"x", 3, 3, 64, ctypes.byref(h)) == -1
 
 
+def test_work_order_validation_without_gpu(degpu_mod):
+    """degpu_work_order / degpu_learned_asolve_ex argument checks come before device work;
+    the host-buffer API refuses a visiting order (its chunks index the batch themselves)."""
+    L = degpu_mod.lib()
+    assert L.degpu_work_order(None, -1, None, None) == -1
+    assert L.degpu_work_order(None, 0, None, None) == 0            # empty: nothing to order
+    assert L.degpu_work_order(None, 10, None, None) == -1          # null buffers
+    assert L.degpu_work_order(None, 1 << 31, None, None) == -1     # more than 2^31-1
+    from degpu import _lib
+    f = degpu_mod.ODEFunction.builtin("lorenz")
+    o = _opts(degpu_mod, degpu_mod.GPUTsit5())
+    pr = _lib.Problems()
+    out = _lib.Outputs()
+    assert L.degpu_learned_asolve_ex(None, None, None, ctypes.byref(pr), ctypes.byref(o), 1e-8, 1.0, 1.0,
+                                     ctypes.byref(out), None) == -1
+    pr.B = -1
+    assert L.degpu_learned_asolve_ex(f.handle(), None, None, ctypes.byref(pr), ctypes.byref(o), 1e-8, 1.0, 1.0,
+                                     ctypes.byref(out), None) == -1
+    pr.B = 0
+    assert L.degpu_learned_asolve_ex(f.handle(), None, None, ctypes.byref(pr), ctypes.byref(o), 1e-8, 1.0, 1.0,
+                                     ctypes.byref(out), None) == 0
+    o.order = 8  # any non-null pointer: refused before it is read
+    assert L.degpu_batch_solve_host(f.handle(), None, None, None, 4, ctypes.byref(o), 1, None, None, 2, None, None,
+                                    None, None) == -1
+    assert "visiting order" in L.degpu_last_error().decode()
+
+
 # ----------------------------------------------------------------------------- host logic
 def test_saveat_normalisation(degpu_mod):
     """lowerlevel_solve.jl:88-102 / 271-306 and test/gpu_kernel_de/conversions.jl."""
