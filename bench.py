@@ -488,7 +488,7 @@ def gpu_arm(args):
             cap = torch.cuda.Stream(dev)
             with torch.cuda.graph(g, stream=cap):
                 call(cap)
-            arms[name] = dict(graph=g, out=out, launches=nlaunch)
+            arms[name] = dict(graph=g, out=out, launches=nlaunch, sm=sm, wm=wm)
 
     for _ in range(args.warmup):
         plain_launch()
@@ -530,9 +530,9 @@ def gpu_arm(args):
     us_h = po["us"].cpu().numpy()
     fl = flops.solve_flops("tsit5", 3, "lorenz", na_h, nr_h, nsaves=B * L)
 
-    # ---------------- end to end through the C ABI with host buffers (plain controller)
-    e2e = None
-    if rank == 0 and not args.no_e2e:
+    # ---------------- end to end through the C ABI with host buffers: inputs copied from
+    # page-locked host memory, outputs written into page-locked host memory, every step
+    def e2e_run(sm, wm, ref_us, arm):
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
         hu0, hp, htsp, hsa = pin(u0), pin(p), pin(tsp), pin(sa)
         hts = torch.empty((B, L), dtype=torch.float64).pin_memory()
@@ -541,11 +541,23 @@ def gpu_arm(args):
         hopt = degpu.api._options(degpu.GPUTsit5(), np.float64, dt=WORKLOAD["dt"], abstol=WORKLOAD["abstol"],
                                   reltol=WORKLOAD["reltol"], saveat_dev=hsa.data_ptr(), nsaveat=L, driver="persistent",
                                   block=block, chunk=chunk)
+        if sm is None and wm is None:
+            api = "degpu_batch_solve_host"
 
-        def e2e_step():
-            _lib.check(_lib.lib().degpu_batch_solve_host(f.handle(), hu0.data_ptr(), hp.data_ptr(), htsp.data_ptr(), B,
-                                                         ctypes.byref(hopt), 1, hts.data_ptr(), hus.data_ptr(), L,
-                                                         hrc.data_ptr(), None, None, sptr))
+            def e2e_step():
+                _lib.check(_lib.lib().degpu_batch_solve_host(f.handle(), hu0.data_ptr(), hp.data_ptr(),
+                                                             htsp.data_ptr(), B, ctypes.byref(hopt), 1, hts.data_ptr(),
+                                                             hus.data_ptr(), L, hrc.data_ptr(), None, None, sptr))
+        else:
+            api = "degpu_learned_batch_solve_host"
+            lo, hi = sm.dt_range if sm is not None else (1e-8, 1e3)
+            smax = sm.scale_range[1] if sm is not None else 1.0
+
+            def e2e_step():
+                _lib.check(_lib.lib().degpu_learned_batch_solve_host(
+                    f.handle(), None if sm is None else sm.h, None if wm is None else wm.h, hu0.data_ptr(),
+                    hp.data_ptr(), htsp.data_ptr(), B, ctypes.byref(hopt), lo, hi, smax, hts.data_ptr(),
+                    hus.data_ptr(), L, hrc.data_ptr(), None, None, sptr))
         for _ in range(min(args.warmup, 2)):
             e2e_step()
         k = max(1, min(args.steps, 5))
@@ -555,12 +567,11 @@ def gpu_arm(args):
         e2e_s = (time.perf_counter() - t0) / k
         h2d = hu0.numel() * 4 + hp.numel() * 4 + htsp.numel() * 8 + hsa.numel() * 8
         d2h = hts.numel() * 8 + hus.numel() * 4 + hrc.numel()
-        same = np.array_equal(hus.numpy().view(np.uint32), us_h.view(np.uint32))
-        e2e = {"value": B / e2e_s, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3, "api": "degpu_batch_solve_host",
-               "transfer": "inputs copied to HBM; outputs written by the solver kernel into the page-locked "
-                           "host buffers over NVLink-C2C",
-               "controller": "plain", "matches_device_run": bool(same)}
+        same = np.array_equal(hus.numpy().view(np.uint32), ref_us.view(np.uint32))
+        return {"value": B / e2e_s, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3, "api": api,
+                "transfer": "inputs copied to HBM; outputs written by the solver kernel into the page-locked "
+                            "host buffers over NVLink-C2C", "arm": arm, "matches_device_run": bool(same)}
 
     if rank != 0:
         _lib.lib().degpu_plan_destroy(plan)
@@ -601,11 +612,11 @@ def gpu_arm(args):
                "sample": f"first {sample} of the {B} trajectories, same workload, OpenMP over trajectories"}
 
     # DRAM bytes per trajectory of the persistent kernel on this workload, from one ncu
-    # capture (dram__bytes_read.sum + dram__bytes_write.sum of a 524,288-trajectory launch,
-    # profiles/persistent_tsit5_lorenz_staged.md) scaled by the trajectories of one launch:
-    # the kernel streams each trajectory's inputs once and writes its output columns once,
-    # so its traffic grows in proportion to B.
-    traffic = TRAFFIC_BYTES_PER_TRAJ * B
+    # capture each in index and in longest-first order (dram__bytes_read.sum +
+    # dram__bytes_write.sum of a 524,288-trajectory launch, profiles/
+    # persistent_tsit5_lorenz_ordered.md) scaled by the trajectories of one launch: the
+    # kernel streams each trajectory's inputs once and writes its output columns once, so
+    # its traffic grows in proportion to B.
 
     # headline: the fastest arm that holds the plain run's error level (p90 within 25 %) and
     # the 1e-4 bar with every trajectory successful; the plain arm otherwise
@@ -629,6 +640,16 @@ def gpu_arm(args):
     # its event-timed step; a learned arm's step also holds the MLP inference and ordering
     # kernels (tens of microseconds), charged to the solve
     achieved = best_rec["flops_per_launch"] / (best_rec["ms_per_step"] * 1e-3) / 1e12
+    traffic = (TRAFFIC_BYTES_PER_TRAJ_ORDERED if best.endswith("_ordered") else TRAFFIC_BYTES_PER_TRAJ) * B
+    # e2e through the host-buffer C ABI on the headline arm's path (and on the plain path)
+    e2e = e2e_plain = None
+    if not args.no_e2e:
+        e2e_plain = e2e_run(None, None, us_h, "plain")
+        if best == "plain":
+            e2e = e2e_plain
+        else:
+            a = arms[best]
+            e2e = e2e_run(a["sm"], a["wm"], a["out"]["us"].cpu().numpy(), best)
     line = {
         "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": best_rec["ms_per_step"],
@@ -652,6 +673,7 @@ def gpu_arm(args):
                      "attempts_per_traj": best_rec["attempts_per_traj"],
                      "plain_index_order_frac": fl / (ms_plain / args.steps * 1e-3) / 1e12 / peak.value},
         "e2e": e2e,
+        "e2e_plain": e2e_plain,
         "cpu_baseline": cpu,
         "other_configs": extras,
         "gpu_launches": args.steps * (1 + sum(a["launches"] for a in arms.values())),
@@ -664,8 +686,41 @@ def gpu_arm(args):
         dist.destroy_process_group()
 
 
+def profile_case(args):
+    """A few launches for a profiler: one index-order solve of the headline workload (which
+    also yields each trajectory's attempts), the longest-first order built from those
+    attempts (the quantity the learned work model predicts, held-out correlation 0.99), and
+    one solve inside the NVTX range "timed" -- select it with
+    ncu --nvtx --nvtx-include "timed/" -k regex:degpu_persistent."""
+    import torch
+
+    import degpu
+    from degpu import learned
+    dev = torch.device("cuda", 0)
+    B = args.trajectories or WORKLOAD["B"]
+    u0, p = make_inputs(B, WORKLOAD["seed"])
+    f = degpu.ODEFunction.builtin("lorenz")
+    probs = degpu.DeviceProblems(f, u0, p, np.tile(np.array(WORKLOAD["tspan"], np.float64), (B, 1)), np.float64, dev)
+    kw = dict(dt=WORKLOAD["dt"], abstol=WORKLOAD["abstol"], reltol=WORKLOAD["reltol"], saveat=saveat_grid(),
+              driver="persistent", block=128, chunk=32)
+    r = degpu.api._solve_device(probs, degpu.GPUTsit5(), True, **kw)
+    order = learned.work_order((r.naccept + r.nreject).float()) if args.profile_case == "ordered" else None
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed")
+    e0.record()
+    r2 = degpu.api._solve_device(probs, degpu.GPUTsit5(), True, order=order, **kw)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    torch.cuda.nvtx.range_pop()
+    same = bool(torch.equal(r.us, r2.us))
+    print(json.dumps({"profile_case": args.profile_case, "trajectories": B, "ms": e0.elapsed_time(e1),
+                      "attempts_per_traj": float((r.naccept + r.nreject).float().mean()), "same_as_index_order": same}))
+
+
 # see the traffic note in gpu_arm
-TRAFFIC_BYTES_PER_TRAJ = (37.9e6 + 183.0e6) / 524288
+TRAFFIC_BYTES_PER_TRAJ = (37.9e6 + 183.1e6) / 524288
+TRAFFIC_BYTES_PER_TRAJ_ORDERED = (77.4e6 + 202.9e6) / 524288
 
 
 def main():
@@ -681,8 +736,13 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--uneven-trajectories", type=int, default=1 << 22)
     ap.add_argument("--train-trajectories", type=int, default=1 << 18)
+    ap.add_argument("--profile-case", choices=["index", "ordered"], default=None,
+                    help="profiler case, not a bench line: one solve of the headline workload inside the "
+                         "NVTX range 'timed', in index order or longest-first by a previous solve's attempts")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        profile_case(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gpu_arm(args)

@@ -33,6 +33,18 @@ namespace degpu {
 typedef DEGPU_TT Tt;  // boundary time type: tspan, saveat and ts are stored as Tt
 constexpr int N = DEGPU_N;
 
+// controller and error-norm quotients: IEEE division in parity mode; in fast mode the
+// SFU reciprocal times the numerator (2 ulp; every divisor here is positive and far below
+// 2^126: error weights >= abstol, step ratios in [1/10, 5], step sizes,
+// dense-output fractions over dt > 1e-14)
+DEGPU_DEV float cdiv(float a, float b) {
+#if DEGPU_PARITY
+  return a / b;
+#else
+  return __fdividef(a, b);
+#endif
+}
+
 // ------------------------------------------------------------------ time inside the kernels
 // Float32 tspan: time is a float and every operation is the reference's Float32 one.
 // FP64 tspan: time is an unevaluated pair (hi, lo) of floats, hi + lo exactly, advanced by
@@ -59,7 +71,7 @@ struct TP {
   static DEGPU_DEV bool lt(T a, T b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
   static DEGPU_DEV bool le(T a, T b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
   static DEGPU_DEV float stage(T t, float c, float dt) { return t.hi + (t.lo + c * dt); }
-  static DEGPU_DEV float theta(T s, T tp, float dt) { return ((s.hi - tp.hi) + (s.lo - tp.lo)) / dt; }
+  static DEGPU_DEV float theta(T s, T tp, float dt) { return cdiv((s.hi - tp.hi) + (s.lo - tp.lo), dt); }
   static DEGPU_DEV float em_theta(T s, T t, float dt) { return (((s.hi - t.hi) + (s.lo - t.lo)) + dt) / dt; }
   static DEGPU_DEV float f32(T t) { return t.hi + t.lo; }
 };
@@ -73,7 +85,7 @@ struct TP {
   static DEGPU_DEV bool lt(T a, T b) { return a < b; }
   static DEGPU_DEV bool le(T a, T b) { return a <= b; }
   static DEGPU_DEV float stage(T t, float c, float dt) { return t + c * dt; }     // t + c*dt
-  static DEGPU_DEV float theta(T s, T tp, float dt) { return (s - tp) / dt; }     // (savet - tprev)/dt
+  static DEGPU_DEV float theta(T s, T tp, float dt) { return cdiv(s - tp, dt); }   // (savet - tprev)/dt
   static DEGPU_DEV float em_theta(T s, T t, float dt) { return (s - (t - dt)) / dt; }
   static DEGPU_DEV float f32(T t) { return t; }
 };
@@ -183,6 +195,7 @@ DEGPU_DEV float ctrl_pow(float x, float y) {
 #endif
 }
 
+
 DEGPU_DEV void rhs(float* du, const float* u, const float* p, float t) { degpu_f<float>(du, u, p, t); }
 
 // DiffEqBase.ODE_DEFAULT_NORM on a static vector: sqrt(sum(abs2, x) / length(x))
@@ -190,7 +203,7 @@ DEGPU_DEV float scaled_norm(const float* e, const float* up, const float* u, flo
   float s = 0.0f;
 #pragma unroll
   for (int i = 0; i < N; i++) {
-    float w = e[i] / (abstol + jl_max(fabsf(up[i]), fabsf(u[i])) * reltol);
+    float w = cdiv(e[i], abstol + jl_max(fabsf(up[i]), fabsf(u[i])) * reltol);
     s = (i == 0) ? w * w : s + w * w;
   }
   return sqrtf(s / (float)N);
@@ -1469,14 +1482,14 @@ DEGPU_DEV bool controller(Lane& L, float EEst, float& dt, Time t) {
   const float qmax = 10.0f, qmin = (float)(1.0 / 5.0), gamma = (float)(9.0 / 10.0), qoldinit = (float)1.0e-4;
   float q11 = 0.0f, q;
   if (EEst == 0.0f) q = 1.0f / qmax;
-  else { q11 = ctrl_pow(EEst, beta1); q = q11 / ctrl_pow(L.qold, beta2); }
+  else { q11 = ctrl_pow(EEst, beta1); q = cdiv(q11, ctrl_pow(L.qold, beta2)); }
   if (EEst > 1.0f) {
-    dt = dt / jl_min(1.0f / qmin, q11 / gamma);
+    dt = cdiv(dt, jl_min(1.0f / qmin, q11 / gamma));
     return false;
   }
   q = jl_max(1.0f / qmax, jl_min(1.0f / qmin, q / gamma));
   L.qold = jl_max(EEst, qoldinit);
-  float dtnew = dt / q;
+  float dtnew = cdiv(dt, q);
   float rem = TP::rem(L.tf, t, dt);
   L.dtnew = jl_min(fabsf(dtnew), fabsf(rem));
   L.dt = dt;

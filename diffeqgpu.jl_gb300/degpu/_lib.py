@@ -107,6 +107,9 @@ SIGNATURES = {
                                                ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                                ctypes.POINTER(Outputs), _P]),
     "degpu_work_order": (ctypes.c_int, [_P, ctypes.c_longlong, _P, _P]),
+    "degpu_learned_batch_solve_host": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, ctypes.c_longlong,
+                                                      ctypes.POINTER(Options), ctypes.c_float, ctypes.c_float,
+                                                      ctypes.c_float, _P, _P, ctypes.c_int, _P, _P, _P, _P]),
     "degpu_learned_asolve_noalloc": (ctypes.c_int, [_P, _P, ctypes.POINTER(Problems), ctypes.POINTER(Options),
                                                     ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                                     ctypes.POINTER(Outputs), _P]),

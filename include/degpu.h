@@ -299,6 +299,17 @@ int degpu_work_order(const float* work, long long B, int* order, void* stream);
 int degpu_learned_asolve_ex(const degpu_rhs* f, const degpu_mlp* m, const degpu_mlp* work_model,
                             const degpu_problems* probs, const degpu_options* opt, float dt_lo, float dt_hi,
                             float s_max, degpu_outputs* out, void* stream);
+/* degpu_batch_solve_host (adaptive ODE solves) with the learned parts of
+ * degpu_learned_asolve_ex: host buffers in and out, the models' inference and the
+ * longest-first order run on the device copies of the inputs (per chunk on the pipelined
+ * path).  Either model may be NULL.  With a work model the outputs are staged in device
+ * memory and copied back in pipelined chunks even when they are page-locked (an ordered
+ * solve's direct writes into host memory arrive scattered; DEGPU_HOST_DIRECT=1 forces
+ * them). */
+int degpu_learned_batch_solve_host(const degpu_rhs* f, const degpu_mlp* step_model, const degpu_mlp* work_model,
+                                   const float* u0, const float* p, const void* tspan, long long B,
+                                   const degpu_options* opt, float dt_lo, float dt_hi, float s_max, void* ts,
+                                   float* us, int L, signed char* retcode, int* naccept, int* nreject, void* stream);
 /* Gradient of the weighted mean squared error over a device batch (target, weight [B][2];
  * weight may be NULL) into the model's gradient buffer; *loss (device scalar, optional). */
 int degpu_mlp_grad(degpu_mlp* m, const float* x, const float* target, const float* weight, long long B, float* loss,

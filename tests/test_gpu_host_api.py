@@ -89,3 +89,52 @@ def test_host_api_chunked_em_and_per_trajectory_saveat(degpu_mod, monkeypatch):
     ts, us, rc, _ = _host_solve(degpu_mod, fl, degpu_mod.GPUTsit5(), u0l, pl, tspl, np.float32, opt, False, 5)
     assert np.array_equal(us.view(np.uint32), rl.us.cpu().numpy().view(np.uint32))
     assert np.array_equal(ts, rl.ts.cpu().numpy())
+
+
+@pytest.mark.parametrize("path", ["direct", "staged_chunked"])
+def test_learned_host_api_matches_device(degpu_mod, monkeypatch, path):
+    """degpu_learned_batch_solve_host (host buffers, step and work models) gives the device
+    solve's bits: the models run on the device copies of the inputs (per chunk on the
+    pipelined path) and the visiting order changes no result."""
+    import torch
+    from degpu import _lib, learned
+    if path != "direct":
+        monkeypatch.setenv("DEGPU_HOST_DIRECT", "0")
+        monkeypatch.setenv("DEGPU_HOST_CHUNK", "40000")
+    B = 120_000
+    rng = np.random.default_rng(21)
+    p = (rng.random((B, 3)) * np.array([10, 28, 8 / 3])).astype(np.float32)
+    u0 = (np.array([1, 0, 0]) + rng.normal(0, 0.1, (B, 3))).astype(np.float32)
+    tsp = np.tile([0.0, 10.0], (B, 1))
+    sa = np.arange(0.0, 10.0001, 0.5)
+    L = len(sa)
+    f = degpu_mod.ODEFunction.builtin("lorenz")
+    sm, _ = learned.fit_step_model(f, u0[:16384], p[:16384], (0.0, 10.0), np.float64, degpu_mod.GPUTsit5(),
+                                   reltol=1e-6, abstol=1e-8, epochs=2)
+    wm, _ = learned.fit_work_model(f, u0[:32768], p[:32768], (0.0, 10.0), np.float64, degpu_mod.GPUTsit5(),
+                                   reltol=1e-6, abstol=1e-8, epochs=2)
+    probs = degpu_mod.DeviceProblems(f, u0, p, tsp, np.float64, torch.device("cuda", 0))
+    r = degpu_mod.api._solve_device(probs, degpu_mod.GPUTsit5(), True, dt=0.1, saveat=sa, abstol=1e-8, reltol=1e-6,
+                                    step_model=sm)
+    torch.cuda.synchronize()
+    pin = (lambda t: t.pin_memory()) if path == "direct" else (lambda t: t)
+    hu0, hp, htsp = [pin(torch.from_numpy(np.ascontiguousarray(a))) for a in (u0, p, tsp)]
+    hts = pin(torch.empty((B, L), dtype=torch.float64))
+    hus = pin(torch.empty((B, L, 3), dtype=torch.float32))
+    hrc = pin(torch.zeros(B, dtype=torch.int8))
+    hna = pin(torch.zeros(B, dtype=torch.int32))
+    hsa = torch.from_numpy(sa.copy()).pin_memory()
+    opt = degpu_mod.api._options(degpu_mod.GPUTsit5(), np.float64, dt=0.1, abstol=1e-8, reltol=1e-6,
+                                 saveat_dev=hsa.data_ptr(), nsaveat=L)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(_lib.lib().degpu_learned_batch_solve_host(
+        f.handle(), sm.h, wm.h, hu0.data_ptr(), hp.data_ptr(), htsp.data_ptr(), B, ctypes.byref(opt), sm.dt_range[0],
+        sm.dt_range[1], sm.scale_range[1], hts.data_ptr(), hus.data_ptr(), L, hrc.data_ptr(), hna.data_ptr(), None, st))
+    assert np.array_equal(hus.numpy().view(np.uint32), r.us.cpu().numpy().view(np.uint32))
+    assert np.array_equal(hts.numpy(), r.ts.cpu().numpy())
+    assert np.array_equal(hrc.numpy(), r.retcode.cpu().numpy()) and np.array_equal(hna.numpy(), r.naccept.cpu().numpy())
+    # models apply to adaptive ODE solves only
+    assert _lib.lib().degpu_learned_batch_solve_host(
+        f.handle(), sm.h, wm.h, hu0.data_ptr(), hp.data_ptr(), htsp.data_ptr(), B, ctypes.byref(
+            degpu_mod.api._options(degpu_mod.GPUEM(), np.float64, dt=0.1)), 1e-8, 1.0, 1.0, hts.data_ptr(),
+        hus.data_ptr(), L, None, None, None, st) == -1
