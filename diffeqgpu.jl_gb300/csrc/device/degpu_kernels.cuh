@@ -155,23 +155,36 @@ enum {
   TS_r42, TS_r43, TS_r44, TS_r52, TS_r53, TS_r54, TS_r62, TS_r63, TS_r64, TS_r72, TS_r73, TS_r74,
   TS_COUNT
 };
-__constant__ float c_tsit5[TS_COUNT] = {
-  (float)0.161, (float)0.327, (float)0.9, (float)0.9800255409045097,
-  (float)0.161, (float)-0.008480655492356989, (float)0.335480655492357,
-  (float)2.897153057105493, (float)-6.359448489975075, (float)4.3622954328695815,
-  (float)5.325864828439257, (float)-11.748883564062828, (float)7.4955393428898365, (float)-0.09249506636175525,
-  (float)5.86145544294642, (float)-12.92096931784711, (float)8.159367898576159, (float)-0.071584973281401, (float)-0.028269050394068383,
-  (float)0.09646076681806523, (float)0.01, (float)0.4798896504144996, (float)1.379008574103742, (float)-3.290069515436081, (float)2.324710524099774,
-  (float)-0.00178001105222577714, (float)-0.0008164344596567469, (float)0.007880878010261995, (float)-0.1447110071732629,
-  (float)0.5823571654525552, (float)-0.45808210592918697, (float)0.015151515151515152,
-  1.0f, (float)-2.763706197274826, (float)2.9132554618219126, (float)-1.0530884977290216,
-  (float)0.13169999999999998, (float)-0.2234, (float)0.1017,
-  (float)3.9302962368947516, (float)-5.941033872131505, (float)2.490627285651253,
-  (float)-12.411077166933676, (float)30.33818863028232, (float)-16.548102889244902,
-  (float)37.50931341651104, (float)-88.1789048947664, (float)47.37952196281928,
-  (float)-27.896526289197286, (float)65.09189467479366, (float)-34.87065786149661,
-  1.5f, -4.0f, 2.5f,
-};
+// the values once (X-macro): FP32 coefficients, and in fast mode the same values duplicated
+// into float2 pairs for the packed FP32 instructions
+#define DEGPU_TSIT5_VALUES(X) \
+  X(0.161) X(0.327) X(0.9) X(0.9800255409045097) \
+  X(0.161) X(-0.008480655492356989) X(0.335480655492357) X(2.897153057105493) \
+  X(-6.359448489975075) X(4.3622954328695815) X(5.325864828439257) X(-11.748883564062828) \
+  X(7.4955393428898365) X(-0.09249506636175525) X(5.86145544294642) X(-12.92096931784711) \
+  X(8.159367898576159) X(-0.071584973281401) X(-0.028269050394068383) X(0.09646076681806523) \
+  X(0.01) X(0.4798896504144996) X(1.379008574103742) X(-3.290069515436081) \
+  X(2.324710524099774) X(-0.00178001105222577714) X(-0.0008164344596567469) X(0.007880878010261995) \
+  X(-0.1447110071732629) X(0.5823571654525552) X(-0.45808210592918697) X(0.015151515151515152) \
+  X(1.0f) X(-2.763706197274826) X(2.9132554618219126) X(-1.0530884977290216) \
+  X(0.13169999999999998) X(-0.2234) X(0.1017) X(3.9302962368947516) \
+  X(-5.941033872131505) X(2.490627285651253) X(-12.411077166933676) X(30.33818863028232) \
+  X(-16.548102889244902) X(37.50931341651104) X(-88.1789048947664) X(47.37952196281928) \
+  X(-27.896526289197286) X(65.09189467479366) X(-34.87065786149661) X(1.5f) \
+  X(-4.0f) X(2.5f)
+#define DEGPU_X_F(v) (float)(v),
+__constant__ float c_tsit5[TS_COUNT] = {DEGPU_TSIT5_VALUES(DEGPU_X_F)};
+// Fast mode on sm_100 and later: Runge-Kutta stage combinations take two state components
+// per instruction with the packed FP32 operations (FFMA2 / FMUL2: two round-to-nearest
+// fused multiply-adds per lane, the same arithmetic as two scalar FMAs); the coefficients
+// are stored as duplicated pairs so that each packed FMA reads one 64-bit constant.
+#if !DEGPU_PARITY && DEGPU_N >= 2 && DEGPU_ALG == 0
+#define DEGPU_PACKED 1
+#define DEGPU_X_F2(v) {(float)(v), (float)(v)},
+__constant__ float2 c_tsit5_2[TS_COUNT] = {DEGPU_TSIT5_VALUES(DEGPU_X_F2)};
+#else
+#define DEGPU_PACKED 0
+#endif
 #define TS(n) c_tsit5[TS_##n]
 #define V7(n) c_vern7[VERN7_##n]
 #define V7X(n) c_vern7x[VERN7X_##n]
@@ -479,11 +492,85 @@ DEGPU_DEV void begin_step(Lane& L, bool first) {
     for (int i = 0; i < N; i++) L.k[0][i] = L.k[6][i];
   }
 }
+#if DEGPU_PACKED
+// sum_j c[J_j] k[j] over k[0..M-1] (left to right), components paired for FFMA2; the last
+// component of an odd N takes the scalar FMA
+template <int... J>
+DEGPU_DEV void ts_sum(float2* s2, float& s1, const float (*k)[N]) {
+  constexpr int idx[sizeof...(J)] = {J...};
+  constexpr int M = sizeof...(J);
+#pragma unroll
+  for (int i = 0; i + 1 < N; i += 2) {
+    float2 acc = __fmul2_rn(c_tsit5_2[idx[0]], make_float2(k[0][i], k[0][i + 1]));
+#pragma unroll
+    for (int j = 1; j < M; j++) acc = __ffma2_rn(c_tsit5_2[idx[j]], make_float2(k[j][i], k[j][i + 1]), acc);
+    s2[i / 2] = acc;
+  }
+  if (N & 1) {
+    float acc = c_tsit5[idx[0]] * k[0][N - 1];
+#pragma unroll
+    for (int j = 1; j < M; j++) acc = fmaf(c_tsit5[idx[j]], k[j][N - 1], acc);
+    s1 = acc;
+  }
+}
+// out = up + dt * sum_j c[J_j] k[j]
+template <int... J>
+DEGPU_DEV void ts_stage(float* out, const float* up, float dt, const float (*k)[N]) {
+  float2 s2[N / 2 > 0 ? N / 2 : 1];
+  float s1 = 0.0f;
+  ts_sum<J...>(s2, s1, k);
+  const float2 dt2 = make_float2(dt, dt);
+#pragma unroll
+  for (int i = 0; i + 1 < N; i += 2) {
+    const float2 r = __ffma2_rn(dt2, s2[i / 2], make_float2(up[i], up[i + 1]));
+    out[i] = r.x;
+    out[i + 1] = r.y;
+  }
+  if (N & 1) out[N - 1] = fmaf(dt, s1, up[N - 1]);
+}
+#endif
+
 template <bool ADAPTIVE>
 DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
   float tmp[N];
   const float* up = L.uprev;
   float(*k)[N] = L.k;
+#if DEGPU_PACKED
+  if (ADAPTIVE) {  // gpu_tsit5_perform_step.jl:104-120, two components per instruction
+    const float a = dt * TS(a21);
+    const float2 a2 = make_float2(a, a);
+#pragma unroll
+    for (int i = 0; i + 1 < N; i += 2) {
+      const float2 r = __ffma2_rn(a2, make_float2(k[0][i], k[0][i + 1]), make_float2(up[i], up[i + 1]));
+      tmp[i] = r.x;
+      tmp[i + 1] = r.y;
+    }
+    if (N & 1) tmp[N - 1] = fmaf(a, k[0][N - 1], up[N - 1]);
+    rhs(k[1], tmp, L.p, tstage(t, TS(c1), dt));
+    ts_stage<TS_a31, TS_a32>(tmp, up, dt, k);
+    rhs(k[2], tmp, L.p, tstage(t, TS(c2), dt));
+    ts_stage<TS_a41, TS_a42, TS_a43>(tmp, up, dt, k);
+    rhs(k[3], tmp, L.p, tstage(t, TS(c3), dt));
+    ts_stage<TS_a51, TS_a52, TS_a53, TS_a54>(tmp, up, dt, k);
+    rhs(k[4], tmp, L.p, tstage(t, TS(c4), dt));
+    ts_stage<TS_a61, TS_a62, TS_a63, TS_a64, TS_a65>(tmp, up, dt, k);
+    rhs(k[5], tmp, L.p, tstage(t, 1.0f, dt));
+    ts_stage<TS_a71, TS_a72, TS_a73, TS_a74, TS_a75, TS_a76>(u, up, dt, k);
+    rhs(k[6], u, L.p, tstage(t, 1.0f, dt));
+    float2 e2[N / 2 > 0 ? N / 2 : 1];
+    float e1 = 0.0f;
+    ts_sum<TS_bt1, TS_bt2, TS_bt3, TS_bt4, TS_bt5, TS_bt6, TS_bt7>(e2, e1, k);
+    const float2 dt2 = make_float2(dt, dt);
+#pragma unroll
+    for (int i = 0; i + 1 < N; i += 2) {
+      const float2 r = __fmul2_rn(dt2, e2[i / 2]);
+      err[i] = r.x;
+      err[i + 1] = r.y;
+    }
+    if (N & 1) err[N - 1] = dt * e1;
+    return;
+  }
+#endif
 #pragma unroll
   for (int i = 0; i < N; i++) tmp[i] = up[i] + (dt * TS(a21)) * k[0][i];
   rhs(k[1], tmp, L.p, tstage(t, TS(c1), dt));
