@@ -53,11 +53,13 @@ def test_tsit5_order_conditions():
 
 
 def test_kernel_tsit5_table_matches_oracle():
-    """The kernels' constant-memory Tsit5 table holds the same FP64 literals as the oracle."""
+    """The kernels' constant-memory Tsit5 table (the value list both the FP32 table and the
+    packed float2 table are built from) holds the same FP64 literals as the oracle."""
     dev = (ROOT / "diffeqgpu.jl_gb300" / "csrc" / "device" / "degpu_kernels.cuh").read_text()
-    block = dev[dev.index("__constant__ float c_tsit5[TS_COUNT]"):]
-    block = block[:block.index("};")]
-    lits = [float(x) for x in re.findall(r"\(float\)(-?[0-9.eE+-]+)|(-?[0-9.]+)f", block) for x in x if x]
+    block = dev[dev.index("#define DEGPU_TSIT5_VALUES(X)"):]
+    block = block[:block.index("#define DEGPU_X_F(")]
+    lits = [float(x.rstrip("f")) for x in re.findall(r"X\((-?[0-9.eE+-]+f?)\)", block)]
+    assert "c_tsit5[TS_COUNT] = {DEGPU_TSIT5_VALUES(DEGPU_X_F)}" in dev
     T = tsit5_fp64()
     order = ["c1", "c2", "c3", "c4"] + [f"a{i}{j}" for i in range(2, 8) for j in range(1, i)] + \
             [f"bt{i}" for i in range(1, 8)] + ["r11", "r12", "r13", "r14"] + \
