@@ -481,7 +481,7 @@ int make_request(const degpu_rhs* f, const degpu_problems* pr, const degpu_optio
   P.dt0 = o->dt0;
   P.tolscale = o->tolscale;
   P.B = pr->B;
-  P.maxiters = o->maxiters > 0 ? o->maxiters : 10000000LL;
+  P.maxiters = (int)std::min<long long>(o->maxiters > 0 ? o->maxiters : 10000000LL, 0x7fffffffLL);
   P.traj_offset = o->traj_offset;
   P.seed = o->seed;
   P.dt = o->dt;

@@ -74,6 +74,8 @@ struct TP {
   static DEGPU_DEV float theta(T s, T tp, float dt) { return cdiv((s.hi - tp.hi) + (s.lo - tp.lo), dt); }
   static DEGPU_DEV float em_theta(T s, T t, float dt) { return (((s.hi - t.hi) + (s.lo - t.lo)) + dt) / dt; }
   static DEGPU_DEV float f32(T t) { return t.hi + t.lo; }
+  // a time that compares false with every time (NaN), for "no further save point"
+  static DEGPU_DEV T never() { DF r; r.hi = __int_as_float(0x7fc00000); r.lo = 0.0f; return r; }
 };
 #else
 struct TP {
@@ -88,6 +90,7 @@ struct TP {
   static DEGPU_DEV float theta(T s, T tp, float dt) { return cdiv(s - tp, dt); }   // (savet - tprev)/dt
   static DEGPU_DEV float em_theta(T s, T t, float dt) { return (s - (t - dt)) / dt; }
   static DEGPU_DEV float f32(T t) { return t; }
+  static DEGPU_DEV T never() { return __int_as_float(0x7fc00000); }  // compares false with every time
 };
 #endif
 typedef TP::T Time;
@@ -182,6 +185,11 @@ __constant__ float c_tsit5[TS_COUNT] = {DEGPU_TSIT5_VALUES(DEGPU_X_F)};
 #define DEGPU_PACKED 1
 #define DEGPU_X_F2(v) {(float)(v), (float)(v)},
 __constant__ float2 c_tsit5_2[TS_COUNT] = {DEGPU_TSIT5_VALUES(DEGPU_X_F2)};
+// dense-output coefficients of the stage pairs (2,3), (4,5), (6,7): {(r_j2, r_j+1,2), (.3), (.4)}
+constexpr float kTs[TS_COUNT] = {DEGPU_TSIT5_VALUES(DEGPU_X_F)};
+#define DEGPU_RP(a, b) {{kTs[TS_r##a##2], kTs[TS_r##b##2]}, {kTs[TS_r##a##3], kTs[TS_r##b##3]}, {kTs[TS_r##a##4], kTs[TS_r##b##4]}}
+__constant__ float2 c_tsit5_rp[3][3] = {DEGPU_RP(2, 3), DEGPU_RP(4, 5), DEGPU_RP(6, 7)};
+#undef DEGPU_RP
 #else
 #define DEGPU_PACKED 0
 #endif
@@ -471,7 +479,7 @@ struct Lane {
   float p[NP];
   Time t, tprev, tf, t0, next_save;
   float dt, dtnew, qold, abstol, reltol;
-  int cur_t, step_idx, nattempt, naccept, nreject, status;
+  int cur_t, step_idx, naccept, nreject, status;
 #if DEGPU_TSTOPS
   int tstops_idx;         // next tstop (0-based integ.tstops_idx)
 #endif
@@ -603,12 +611,25 @@ DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
 // nonstiff/interpolants.jl:372-387 with SimpleDiffEq.bθs (Horner)
 DEGPU_DEV void interp(const Lane& L, float th, float dt, float* out) {
   float b0 = (((TS(r14) * th + TS(r13)) * th + TS(r12)) * th + TS(r11)) * th;
+#if DEGPU_PACKED
+  // the six same-shaped polynomials two at a time (FFMA2 / FMUL2, the scalar Horner steps)
+  const float2 t2 = make_float2(th, th);
+  float2 bp[3];
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    float2 a = __ffma2_rn(c_tsit5_rp[q][2], t2, c_tsit5_rp[q][1]);
+    a = __ffma2_rn(a, t2, c_tsit5_rp[q][0]);
+    bp[q] = __fmul2_rn(__fmul2_rn(a, t2), t2);
+  }
+  const float b1 = bp[0].x, b2 = bp[0].y, b3 = bp[1].x, b4 = bp[1].y, b5 = bp[2].x, b6 = bp[2].y;
+#else
   float b1 = (((TS(r24) * th + TS(r23)) * th + TS(r22)) * th) * th;
   float b2 = (((TS(r34) * th + TS(r33)) * th + TS(r32)) * th) * th;
   float b3 = (((TS(r44) * th + TS(r43)) * th + TS(r42)) * th) * th;
   float b4 = (((TS(r54) * th + TS(r53)) * th + TS(r52)) * th) * th;
   float b5 = (((TS(r64) * th + TS(r63)) * th + TS(r62)) * th) * th;
   float b6 = (((TS(r74) * th + TS(r73)) * th + TS(r72)) * th) * th;
+#endif
 #pragma unroll
   for (int i = 0; i < N; i++)
     out[i] = L.uprev[i] + dt * (b0 * L.k[0][i] + b1 * L.k[1][i] + b2 * L.k[2][i] + b3 * L.k[3][i] + b4 * L.k[4][i] + b5 * L.k[5][i] + b6 * L.k[6][i]);
@@ -1521,14 +1542,15 @@ DEGPU_DEV void lane_init(Lane& L, const Io& io, int i) {
   L.qold = (float)1.0e-4;
   L.cur_t = 0;
   L.step_idx = 1;
-  L.nattempt = 0;
   L.naccept = 0;
   L.nreject = 0;
   L.status = DEGPU_RET_DEFAULT;
   if (io.P.nsaveat) {
     const Tt s0 = io.saveat(i, 0);
     if (t0_in == s0) { L.cur_t = 1; io.store_u(i, 0, L.u); }
-    L.next_save = io.save_time(i, L.cur_t < io.P.nsaveat ? L.cur_t : 0);
+    // the next save time; once every point is saved a NaN, which no time reaches (no index
+    // test in the step loop)
+    L.next_save = L.cur_t < io.P.nsaveat ? io.save_time(i, L.cur_t) : TP::never();
   } else {
     io.store_u(i, 0, L.u);
   }
@@ -1546,15 +1568,14 @@ DEGPU_DEV void lane_init(Lane& L, const Io& io, int i) {
 DEGPU_DEV void save_values(Lane& L, const Io& io, int i, bool save_everystep) {
   if (io.P.nsaveat) {
     // the next save time is cached in registers: one compare per step, no global load
-    while (L.cur_t < io.P.nsaveat && TP::le(L.next_save, L.t)) {
+    // (L == nsaveat: the host rejects other output sizes with saveat)
+    while (TP::le(L.next_save, L.t)) {
       float th = TP::theta(L.next_save, L.tprev, L.dt);
-      if (L.cur_t < io.P.L) {
-        float v[N];
-        interp(L, th, L.dt, v);
-        io.store_u(i, L.cur_t, v);
-      }
+      float v[N];
+      interp(L, th, L.dt, v);
+      io.store_u(i, L.cur_t, v);
       L.cur_t++;
-      if (L.cur_t < io.P.nsaveat) L.next_save = io.save_time(i, L.cur_t);
+      L.next_save = L.cur_t < io.P.nsaveat ? io.save_time(i, L.cur_t) : TP::never();
     }
   } else if (save_everystep) {
     if (L.step_idx < io.P.L) { io.store_u(i, L.step_idx, L.u); io.ts(i)[L.step_idx] = TP::out(L.t); }
@@ -1827,7 +1848,7 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, int i) {
   if (ADAPTIVE) {
     float dt = L.dtnew;
     if (dt < 1.0e-14f) { L.status = DEGPU_RET_DTLESSTHANMIN; return true; }
-    if (++L.nattempt > io.P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
+    if (L.naccept + L.nreject >= io.P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }  // attempts so far
     attempt<true>(L, t, dt, unew, err);
     float EEst = scaled_norm(err, L.uprev, unew, L.abstol, L.reltol);
 #if !DEGPU_PARITY
@@ -1849,7 +1870,7 @@ DEGPU_DEV bool advance(Lane& L, const Io& io, int i) {
     }
 #endif
   } else {
-    if (++L.nattempt > io.P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }
+    if (L.naccept >= io.P.maxiters) { L.status = DEGPU_RET_MAXITERS; return true; }  // steps so far
     float dt = L.dt;
     L.tprev = t;
 #if DEGPU_TSTOPS

@@ -34,7 +34,7 @@ typedef struct degpu_kparams {
   float* dt_first;         /* [B] or null: first accepted dt (step-size trace) */
   unsigned long long* work; /* persistent driver: work[0] = next unclaimed trajectory */
   long long B;
-  long long maxiters;     /* cap on step attempts per trajectory */
+  int maxiters;           /* cap on step attempts per trajectory (host-clamped to 2^31-1) */
   long long traj_offset;  /* global index of trajectory 0 (noise streams, shards) */
   unsigned long long seed;/* EM noise key */
   double dt;              /* fixed dt or initial dt, converted to Tt in the kernel */
