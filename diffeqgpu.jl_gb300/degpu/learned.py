@@ -243,7 +243,8 @@ def scale_targets(errs, scales, target_err):
 
 
 def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_quantile=0.9, safety=0.5,
-                   scales=(1, 2, 4, 8, 16, 32, 64), epochs=8, seed=0, calib_frac=0.125, calib_margin=1.1, log=None):
+                   scales=(1, 2, 4, 8, 16, 32, 64), epochs=8, seed=0, calib_frac=0.125, calib_margin=1.1, log=None,
+                   expectile=0.1, expectile_rounds=3):
     """Train a StepSizeModel on the plain solver's traces of the given ensemble.
 
     The common error target is `safety` times the `target_quantile` of the plain run's
@@ -253,7 +254,13 @@ def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_qu
     shifted down by the smallest margin at which the learned run's error-proxy quantile
     is within `calib_margin` of the plain run's (regression to the mean would otherwise
     over-relax the most sensitive trajectories; the margin absorbs the few-percent change
-    that a different initial step alone makes to the quantile)."""
+    that a different initial step alone makes to the quantile).
+
+    With `expectile` set, the scale output is then refined towards that expectile of the
+    targets (asymmetric squared loss by iteratively reweighted least squares: residuals
+    where the network over-relaxes weigh 1 - expectile, the others expectile), so that its
+    predictions stay below the targets where they are uncertain and the calibration shift
+    that follows can be small."""
     import torch
 
     from .api import DeviceProblems, _solve_device
@@ -271,6 +278,14 @@ def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_qu
     m = StepSizeModel(x.shape[1], seed=seed)
     m.scale_range = (1.0, float(max(scales)))
     m.fit(x, y, w, epochs=epochs, seed=seed, log=log)
+    if expectile is not None and expectile_rounds > 0:
+        dev = torch.device("cuda", torch.cuda.current_device())
+        xd = torch.as_tensor(x, device=dev)
+        for r in range(expectile_rounds):
+            yp = m.infer(xd, raw=True)[:, 1].cpu().numpy()
+            w[:, 1] = np.where(yp > y[:, 1], 1.0 - expectile, expectile) * 2.0
+            # the network already predicts in the targets' units: no target standardisation
+            m.fit(x, y, w, epochs=max(2, epochs // 2), lr=1e-3, seed=seed + 1 + r, log=log, normalize_targets=False)
     info = {"target_err": target, "err_proxy_median": float(np.median(e1)), "n_train": int(ut.shape[0]),
             "scale_target_median": float(np.median(s)), "scale_target_mean_log": float(np.log(s).mean())}
     if nc > 0:
