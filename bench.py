@@ -719,8 +719,8 @@ def profile_case(args):
 
 
 # see the traffic note in gpu_arm
-TRAFFIC_BYTES_PER_TRAJ = (37.9e6 + 183.1e6) / 524288
-TRAFFIC_BYTES_PER_TRAJ_ORDERED = (77.4e6 + 202.9e6) / 524288
+TRAFFIC_BYTES_PER_TRAJ = (34.8e6 + 178.9e6) / 524288
+TRAFFIC_BYTES_PER_TRAJ_ORDERED = (76.0e6 + 200.0e6) / 524288
 
 
 def main():
