@@ -265,6 +265,35 @@ def extra_configs(args, dev, flush):
             "retcode_counts": {str(int(c)): int(n) for c, n in zip(*np.unique(r.retcode.cpu().numpy(),
                                                                               return_counts=True))}}
 
+    # learned step control on the Robertson ensemble (Rodas5P): step and work models trained
+    # on 65,536 fresh draws of the same distribution, evaluated on the 262,144 above
+    if not args.no_learned:
+        from degpu import learned
+        kw_ = (np.array([0.04, 3e7, 1e4]) * np.exp(np.random.default_rng(44).normal(0, 0.3, (1 << 16, 3)))).astype(np.float32)
+        u0w_ = np.tile(np.array([1, 0, 0], np.float32), (1 << 16, 1))
+        sm2, sinfo2 = learned.fit_step_model(fr, u0w_, kw_, (0.0, 1e5), np.float64, degpu.GPURodas5P(), reltol=1e-4,
+                                             abstol=1e-7, dt=1e-3)
+        wm2, _ = learned.fit_work_model(fr, u0w_, kw_, (0.0, 1e5), np.float64, degpu.GPURodas5P(), reltol=1e-4,
+                                        abstol=1e-7, dt=1e-3, step_model=sm2)
+        lr2 = {}
+        for arm, kw2 in (("plain", {}), ("learned", dict(step_model=sm2, work_model=wm2))):
+            def run2l(kw2=kw2):
+                holder["r"] = degpu.api._solve_device(pr2, degpu.GPURodas5P(), True, dt=1e-3, saveat=sa2, abstol=1e-7,
+                                                      reltol=1e-4, driver="persistent", **kw2)
+            ms = time_solve(run2l)
+            r = holder["r"]
+            na, nr = r.naccept.cpu().numpy(), r.nreject.cpu().numpy()
+            yf = r.us[:, -1].cpu().numpy()[idx2].astype(np.float64)
+            err = np.abs(yf[:, [0, 2]] - ref2[:, 0, [0, 2]]) / np.abs(ref2[:, 0, [0, 2]])
+            lr2[arm] = {"trajectories_per_s": B2 / (ms * 1e-3), "ms": ms, "attempts_per_traj": float((na + nr).mean()),
+                        "reject_frac": float(nr.sum() / max(1, (na + nr).sum())),
+                        "rel_err_median": float(np.median(err)), "rel_err_p90": float(np.quantile(err, 0.9)),
+                        "retcodes_ok": bool((r.retcode.cpu().numpy() == 1).all())}
+        lr2["learned"]["speedup_vs_plain"] = lr2["learned"]["trajectories_per_s"] / lr2["plain"]["trajectories_per_s"]
+        lr2["learned"]["calib_log_scale_shift"] = sinfo2.get("calib_log_scale_shift")
+        lr2["learned"]["includes"] = "step- and work-model inference + ordering kernels"
+        res["learned_robertson_262k_rodas5p"] = lr2
+
     # uneven Lorenz batch: rho ~ U(0,100), tEnd ~ U(1,20), final state only
     B3 = args.uneven_trajectories
     p3 = np.stack([np.full(B3, 10.0), rng.uniform(0, 100, B3), np.full(B3, 8 / 3)], 1).astype(np.float32)
@@ -306,25 +335,67 @@ def extra_configs(args, dev, flush):
                                       "includes": "work-model inference + ordering kernels"}
         out3["ordered_speedup_vs_persistent"] = (out3["persistent_ordered"]["trajectories_per_s"]
                                                  / out3["persistent"]["trajectories_per_s"])
+        # learned step control on this distribution (trained on the same 262,144 fresh draws,
+        # span tEnd as an input), evaluated on the 4,194,304-trajectory batch: rejected-step
+        # fraction, throughput and FP64-oracle error against the plain controller
+        u0w = np.tile(np.array([1, 0, 0], np.float32), (Bw, 1))
+        sm3, sinfo3 = learned.fit_step_model(f, u0w, pw, tw, np.float64, degpu.GPUTsit5(), reltol=1e-6, abstol=1e-8)
+        wm3l, _ = learned.fit_work_model(f, u0w, pw, tw, np.float64, degpu.GPUTsit5(), reltol=1e-6, abstol=1e-8,
+                                         step_model=sm3)
+
+        def run3l():
+            holder["r"] = degpu.api._solve_device(pr3, degpu.GPUTsit5(), True, dt=0.1, abstol=1e-8, reltol=1e-6,
+                                                  driver="persistent", step_model=sm3, work_model=wm3l)
+        ms = time_solve(run3l, reps=2)
+        rl = holder["r"]
+        run3()  # the plain persistent solve again, for its outputs
+        rp = holder["r"]
+        idx3 = np.arange(0, B3, B3 // 1024)[:1024]
+        u3s, p3s = u03[idx3].astype(np.float64), p3[idx3].astype(np.float64)
+        stops = tsp3[idx3, 1:2]
+        ref3, _ = oracle.vern9("lorenz", u3s, p3s, 0.0, stops, rtol=1e-12, atol=1e-14)
+        # members an FP32 solve can resolve: a perturbation of u0 at the FP32 rounding level
+        # (1e-6 relative) moves the FP64 final state by less than 1e-3 (over spans up to 20
+        # the transiently chaotic members otherwise settle on either fixed point)
+        pert3, _ = oracle.vern9("lorenz", u3s * (1 + 1e-6), p3s, 0.0, stops, rtol=1e-12, atol=1e-14)
+        nref3 = np.maximum(np.linalg.norm(ref3[:, 0], axis=1), 1e-3)
+        stable3 = np.linalg.norm(ref3[:, 0] - pert3[:, 0], axis=1) / nref3 < 1e-3
+
+        def err3(r):
+            e = np.linalg.norm(r.us[:, 1].cpu().numpy()[idx3].astype(np.float64) - ref3[:, 0], axis=1) / nref3
+            e = e[stable3]
+            return {"median": float(np.median(e)), "p90": float(np.quantile(e, 0.9)), "n_stable": int(stable3.sum())}
+
+        def stats(r):
+            na_, nr_ = r.naccept.cpu().numpy(), r.nreject.cpu().numpy()
+            return {"attempts_per_traj": float((na_ + nr_).mean()),
+                    "reject_frac": float(nr_.sum() / max(1, (na_ + nr_).sum())),
+                    "retcodes_ok": bool((r.retcode.cpu().numpy() == 1).all())}
+        out3["learned"] = {"trajectories_per_s": B3 / (ms * 1e-3), "ms": ms, **stats(rl), "oracle_error": err3(rl),
+                           "speedup_vs_persistent": (B3 / (ms * 1e-3)) / out3["persistent"]["trajectories_per_s"],
+                           "includes": "step- and work-model inference + ordering kernels",
+                           "calib_log_scale_shift": sinfo3.get("calib_log_scale_shift")}
+        out3["persistent"].update({**stats(rp), "oracle_error": err3(rp)})
     res[f"uneven_lorenz_{B3}"] = out3
 
-    # the adaptive Lorenz ensemble with GPUVern9 (the headline tolerances; FP32 state, so
-    # tolerances below ~1e-7 would only measure round-off)
+    # the adaptive Lorenz ensemble with GPUVern7 and GPUVern9 (the headline tolerances; FP32
+    # state, so tolerances below ~1e-7 would only measure round-off)
     B5 = 1 << 20
     u05, p05 = make_inputs(B5, WORKLOAD["seed"] + 5)
     pr5 = degpu.DeviceProblems(f, u05, p05, np.tile(np.array(WORKLOAD["tspan"], np.float64), (B5, 1)), np.float64, dev)
     sa5 = saveat_grid()
 
-    def run5():
-        holder["r"] = degpu.api._solve_device(pr5, degpu.GPUVern9(), True, dt=0.1, saveat=sa5,
-                                              abstol=WORKLOAD["abstol"], reltol=WORKLOAD["reltol"])
-    ms = time_solve(run5)
-    r = holder["r"]
-    na, nr = r.naccept.cpu().numpy(), r.nreject.cpu().numpy()
-    fl = flops.solve_flops("vern9", 3, "lorenz", na, nr, nsaves=B5 * len(sa5))
-    res["lorenz_vern9_1M"] = {
-        "trajectories_per_s": B5 / (ms * 1e-3), "ms": ms, "attempts_per_traj": float((na + nr).mean()),
-        "fp32_tflops": fl / (ms * 1e-3) / 1e12, "retcodes_ok": bool((r.retcode.cpu().numpy() == 1).all())}
+    for vname, valg in (("vern7", degpu.GPUVern7()), ("vern9", degpu.GPUVern9())):
+        def run5(valg=valg):
+            holder["r"] = degpu.api._solve_device(pr5, valg, True, dt=0.1, saveat=sa5,
+                                                  abstol=WORKLOAD["abstol"], reltol=WORKLOAD["reltol"])
+        ms = time_solve(run5)
+        r = holder["r"]
+        na, nr = r.naccept.cpu().numpy(), r.nreject.cpu().numpy()
+        fl = flops.solve_flops(vname, 3, "lorenz", na, nr, nsaves=B5 * len(sa5))
+        res[f"lorenz_{vname}_1M"] = {
+            "trajectories_per_s": B5 / (ms * 1e-3), "ms": ms, "attempts_per_traj": float((na + nr).mean()),
+            "fp32_tflops": fl / (ms * 1e-3) / 1e12, "retcodes_ok": bool((r.retcode.cpu().numpy() == 1).all())}
 
     # the public Python API end to end (degpu.solve on a bulk-built EnsembleProblem: host
     # arrays in, page-locked host ts/us out, lazy per-trajectory solutions)

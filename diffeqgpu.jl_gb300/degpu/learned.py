@@ -244,7 +244,7 @@ def scale_targets(errs, scales, target_err):
 
 def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_quantile=0.9, safety=0.5,
                    scales=(1, 2, 4, 8, 16, 32, 64), epochs=8, seed=0, calib_frac=0.125, calib_margin=1.1, log=None,
-                   expectile=0.1, expectile_rounds=3):
+                   expectile=0.1, expectile_rounds=3, dt=0.1, resolved=1e-3):
     """Train a StepSizeModel on the plain solver's traces of the given ensemble.
 
     The common error target is `safety` times the `target_quantile` of the plain run's
@@ -260,21 +260,35 @@ def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_qu
     targets (asymmetric squared loss by iteratively reweighted least squares: residuals
     where the network over-relaxes weigh 1 - expectile, the others expectile), so that its
     predictions stay below the targets where they are uncertain and the calibration shift
-    that follows can be small."""
+    that follows can be small.
+
+    `tspan` is one (t0, tf) or per-trajectory [B, 2]; in the second case the span tf - t0
+    is a model input too.  `dt` is the plain solver's initial step.
+
+    Members whose plain error proxy is above `resolved` (chaotic ones over long spans, where
+    no FP32 solve tracks the tighter one) neither set the common error target nor enter the
+    calibration quantiles, and their scale target is 1: the error level the learned run
+    must hold is that of the members the plain run actually resolves."""
     import torch
 
     from .api import DeviceProblems, _solve_device
     B = u0.shape[0]
     nc = int(B * calib_frac)
+    per_traj = np.ndim(tspan) == 2
+    tsp_all = np.asarray(tspan) if per_traj else np.broadcast_to(np.asarray(tspan, dtype=time_type), (B, 2))
+    span = (tsp_all[:, 1].astype(np.float64) - tsp_all[:, 0]) if per_traj else None
     ut, pt, uc, pc = u0[nc:], p[nc:], u0[:nc], p[:nc]
-    dtf, errs, _ = solver_traces(f, ut, pt, tspan, time_type, alg, reltol=reltol, abstol=abstol, scales=scales)
-    e1 = errs[0][np.isfinite(errs[0])]
+    tt, tc = tsp_all[nc:], tsp_all[:nc]
+    st, sc_span = (span[nc:], span[:nc]) if per_traj else (None, None)
+    dtf, errs, _ = solver_traces(f, ut, pt, tt, time_type, alg, reltol=reltol, abstol=abstol, scales=scales, dt=dt)
+    res = np.isfinite(errs[0]) & (errs[0] <= resolved)
+    e1 = errs[0][res] if res.any() else errs[0][np.isfinite(errs[0])]
     target = safety * float(np.quantile(e1, target_quantile))
-    s = scale_targets(errs, scales, target)
+    s = np.where(res, scale_targets(errs, scales, target), 1.0)
     ok = np.isfinite(dtf) & (dtf > 0)
     y = np.stack([np.log(np.where(ok, dtf, 1.0)), np.log(s)], 1).astype(np.float32)
     w = np.stack([ok, np.ones_like(ok)], 1).astype(np.float32)
-    x = features(ut, pt, np.full(ut.shape[0], reltol))
+    x = features(ut, pt, np.full(ut.shape[0], reltol), st)
     m = StepSizeModel(x.shape[1], seed=seed)
     m.scale_range = (1.0, float(max(scales)))
     m.fit(x, y, w, epochs=epochs, seed=seed, log=log)
@@ -287,26 +301,32 @@ def fit_step_model(f, u0, p, tspan, time_type, alg, *, reltol, abstol, target_qu
             # the network already predicts in the targets' units: no target standardisation
             m.fit(x, y, w, epochs=max(2, epochs // 2), lr=1e-3, seed=seed + 1 + r, log=log, normalize_targets=False)
     info = {"target_err": target, "err_proxy_median": float(np.median(e1)), "n_train": int(ut.shape[0]),
+            "resolved_frac": float(res.mean()),
             "scale_target_median": float(np.median(s)), "scale_target_mean_log": float(np.log(s).mean())}
     if nc > 0:
         dev = torch.device("cuda", torch.cuda.current_device())
-        tsp = np.broadcast_to(np.asarray(tspan, dtype=time_type), (nc, 2))
-        probs = DeviceProblems(f, uc, pc, tsp, time_type, dev)
-        ref = _solve_device(probs, alg, True, dt=0.1, abstol=abstol / 64, reltol=reltol / 64)
+        probs = DeviceProblems(f, uc, pc, np.ascontiguousarray(tc), time_type, dev)
+        ref = _solve_device(probs, alg, True, dt=dt, abstol=abstol / 64, reltol=reltol / 64)
         ur = ref.us[:, 1].double()
         nr = ur.norm(dim=1).clamp_min(1e-3)
 
+        rplain = _solve_device(probs, alg, True, dt=dt, abstol=abstol, reltol=reltol)
+        e_plain = (rplain.us[:, 1].double() - ur).norm(dim=1) / nr
+        keep = e_plain <= resolved
+        if int(keep.sum()) < 16:
+            keep = torch.isfinite(e_plain)
+
         def proxy(r):
             e = (r.us[:, 1].double() - ur).norm(dim=1) / nr
-            return float(torch.quantile(e, target_quantile))
-        q_plain = proxy(_solve_device(probs, alg, True, dt=0.1, abstol=abstol, reltol=reltol))
-        xc = torch.as_tensor(features(uc, pc, np.full(nc, reltol)), device=dev)
+            return float(torch.quantile(e[keep], target_quantile))
+        q_plain = proxy(rplain)
+        xc = torch.as_tensor(features(uc, pc, np.full(nc, reltol), sc_span), device=dev)
         y_raw = m.infer(xc, raw=True)
         dt0 = torch.exp(y_raw[:, 0]).clamp(*m.dt_range).contiguous()
         shift = None
         for delta in np.arange(0.0, 4.01, 0.25):
             sc = torch.exp(y_raw[:, 1] - float(delta)).clamp(*m.scale_range).contiguous()
-            q = proxy(_solve_device(probs, alg, True, dt=0.1, abstol=abstol, reltol=reltol, dt0=dt0, tolscale=sc))
+            q = proxy(_solve_device(probs, alg, True, dt=dt, abstol=abstol, reltol=reltol, dt0=dt0, tolscale=sc))
             if q <= calib_margin * q_plain:
                 shift = float(delta)
                 break
