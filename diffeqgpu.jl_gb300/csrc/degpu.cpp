@@ -952,8 +952,8 @@ int degpu_learned_asolve_ex(const degpu_rhs* f, const degpu_mlp* m, const degpu_
   if (m && (!(s_max >= 1.0f) || !(dt_lo > 0.0f) || !(dt_hi >= dt_lo))) return fail(DEGPU_E_INVALID, "bad dt / scale clamp");
   cudaStream_t s = (cudaStream_t)stream;
   const size_t B = (size_t)probs->B;
-  // scratch: [dt0 | tolscale] (step model), [predicted work | unused | order] (work model)
-  const size_t n_step = m ? 2 * B : 0, n_work = work_model ? 3 * B : 0;
+  // scratch: [dt0 | tolscale] (step model), [predicted work | order] (work model)
+  const size_t n_step = m ? 2 * B : 0, n_work = work_model ? 2 * B : 0;
   float* scratch = nullptr;
   int rc = lib_alloc((void**)&scratch, sizeof(float) * (n_step + n_work), s);
   if (rc) return rc;
@@ -973,7 +973,7 @@ int degpu_learned_asolve_ex(const degpu_rhs* f, const degpu_mlp* m, const degpu_
   if (!rc && work_model) {
     // predicted attempts = exp(first output), clamped to [1, 2^31]; the second output is unused
     float* work = scratch + n_step;
-    int* order = reinterpret_cast<int*>(scratch + n_step + 2 * B);
+    int* order = reinterpret_cast<int*>(scratch + n_step + B);
     rc = degpu_internal_mlp_infer_problems(work_model, probs->u0, f->N, probs->p, f->P, probs->tspan, span_f64,
                                            (float)opt->reltol, probs->B, work, nullptr, 1.0f, 2147483648.0f, 1.0f,
                                            1.0f, stream);

@@ -115,7 +115,8 @@ function flatten(probs, ::Type{Tt}) where {Tt}
 end
 
 function _solve(f::CudaRHS, probs, alg::Symbol, adaptive::Bool; dt, saveat = nothing, save_everystep,
-        abstol = 1.0f-6, reltol = 1.0f-3, Tt = Float32, mode = 0, driver = 0, maxiters = 0, seed = 0)
+        abstol = 1.0f-6, reltol = 1.0f-3, Tt = Float32, mode = 0, driver = 0, maxiters = 0, seed = 0,
+        order = nothing)
     B = length(probs)
     u0, p, tspan = flatten(probs, Tt)
     sa = saveat === nothing ? nothing : CuArray(Tt.(collect(saveat)))
@@ -127,13 +128,22 @@ function _solve(f::CudaRHS, probs, alg::Symbol, adaptive::Bool; dt, saveat = not
     opt = Options(alg = ALG[alg], time_type = Tt === Float64 ? 1 : 0, mode = mode, driver = driver,
         save_everystep = save_everystep, nsaveat = sa === nothing ? 0 : length(sa),
         saveat = sa === nothing ? C_NULL : pointer(sa), dt = dt, abstol = abstol, reltol = reltol,
-        maxiters = maxiters, seed = seed)
+        maxiters = maxiters, seed = seed, order = order === nothing ? C_NULL : pointer(order))
     prs = Problems(pointer(u0), pointer(p), pointer(tspan), B)
     out = Outputs(pointer(ts), Ptr{Float32}(pointer(us)), L, C_NULL, C_NULL, C_NULL, C_NULL)
     fn = alg === :GPUEM ? :degpu_vectorized_solve_sde : adaptive ? :degpu_vectorized_asolve : :degpu_vectorized_solve
     check(ccall((fn, libdegpu), Cint, (Ptr{Cvoid}, Ref{Problems}, Ref{Options}, Ref{Outputs}, Ptr{Cvoid}),
         f.handle, prs, opt, out, CUDA.stream().handle))
     return ts, us
+end
+
+# Longest-first visiting order for the persistent driver from a per-trajectory work estimate
+# (e.g. a work model's predicted attempts); pass it as `order` to vectorized_asolve.
+function work_order(work::CuVector{Float32})
+    order = CuVector{Cint}(undef, length(work))
+    check(ccall((:degpu_work_order, libdegpu), Cint, (CuPtr{Float32}, Clonglong, CuPtr{Cint}, Ptr{Cvoid}),
+        work, length(work), order, CUDA.stream().handle))
+    return order
 end
 
 vectorized_solve(f::CudaRHS, probs, alg::Symbol; dt, saveat = nothing, save_everystep = true, kw...) =

@@ -293,9 +293,9 @@ int degpu_work_order(const float* work, long long B, int* order, void* stream);
  * degpu_mlp whose first output is the predicted log step attempts of this solve, turned
  * into a visiting order by degpu_work_order.  Either model may take one more input after
  * log10 reltol, the span tf - t0 of each trajectory's tspan (input width N + P + 2), for
- * ensembles with per-trajectory tspans.  Scratch: 8 bytes per trajectory per model, plus 4
- * for the order, from the stream-ordered allocator.  opt->dt0 / tolscale / order are
- * ignored. */
+ * ensembles with per-trajectory tspans.  Scratch: 8 bytes per trajectory per model (the
+ * work model's 8 are its prediction and the order), from the stream-ordered allocator.
+ * opt->dt0 / tolscale / order are ignored. */
 int degpu_learned_asolve_ex(const degpu_rhs* f, const degpu_mlp* m, const degpu_mlp* work_model,
                             const degpu_problems* probs, const degpu_options* opt, float dt_lo, float dt_hi,
                             float s_max, degpu_outputs* out, void* stream);

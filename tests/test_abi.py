@@ -193,6 +193,15 @@ def test_work_order_validation_without_gpu(degpu_mod):
     pr.B = 0
     assert L.degpu_learned_asolve_ex(f.handle(), None, None, ctypes.byref(pr), ctypes.byref(o), 1e-8, 1.0, 1.0,
                                      ctypes.byref(out), None) == 0
+    # the learned host-buffer solve takes models for adaptive ODE solves only (refused before
+    # any device work); with no model it is the plain host solve
+    em = _opts(degpu_mod, degpu_mod.GPUEM())
+    fake_model = ctypes.c_void_p(8)  # never dereferenced: validation fails first
+    assert L.degpu_learned_batch_solve_host(f.handle(), fake_model, None, None, None, None, 4, ctypes.byref(em), 1e-8,
+                                            1.0, 1.0, None, None, 2, None, None, None, None) == -1
+    assert "adaptive ODE" in L.degpu_last_error().decode()
+    assert L.degpu_learned_batch_solve_host(f.handle(), None, None, None, None, None, 0, ctypes.byref(o), 1e-8, 1.0,
+                                            1.0, None, None, 2, None, None, None, None) == 0
     o.order = 8  # any non-null pointer: refused before it is read
     assert L.degpu_batch_solve_host(f.handle(), None, None, None, 4, ctypes.byref(o), 1, None, None, 2, None, None,
                                     None, None) == -1
