@@ -24,6 +24,7 @@ import ctypes
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 from pathlib import Path
@@ -112,7 +113,8 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index=0):
-        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+        # raw samples; the summary goes into the bench line.  DEGPU_CLOCKS_DIR keeps them
+        self.path = Path(os.environ.get("DEGPU_CLOCKS_DIR", tempfile.gettempdir())) / f"clocks_bench_{os.getpid()}.csv"
         self.proc = None
         self.gpu = gpu_index
         self.t0 = self.t1 = None
