@@ -14,6 +14,16 @@
 //   DEGPU_LINSOLVE_REFINE   fast mode: 1 = one compensated (double-float) residual refinement
 // The reference's semantics (file:line in DiffEqGPU.jl) are cited at each piece.
 #pragma once
+// Fast mode on sm_100 and later: explicit Runge-Kutta stage sums (Tsit5, Vern7, Vern9) take
+// two state components per instruction with the packed FP32 operations (FFMA2 / FMUL2: two
+// round-to-nearest fused multiply-adds per lane, the arithmetic of two scalar FMAs); their
+// coefficients are also stored as duplicated pairs, one 64-bit constant per packed FMA.
+#if !DEGPU_PARITY && DEGPU_N >= 2 && (DEGPU_ALG == 0 || DEGPU_ALG == 1 || DEGPU_ALG == 6)
+#define DEGPU_PACKED 1
+#else
+#define DEGPU_PACKED 0
+#endif
+#define DEGPU_PACKED_TABLES DEGPU_PACKED
 #include "tableaus_gen.cuh"
 
 #ifndef DEGPU_N
@@ -177,12 +187,9 @@ enum {
   X(-4.0f) X(2.5f)
 #define DEGPU_X_F(v) (float)(v),
 __constant__ float c_tsit5[TS_COUNT] = {DEGPU_TSIT5_VALUES(DEGPU_X_F)};
-// Fast mode on sm_100 and later: Runge-Kutta stage combinations take two state components
-// per instruction with the packed FP32 operations (FFMA2 / FMUL2: two round-to-nearest
-// fused multiply-adds per lane, the same arithmetic as two scalar FMAs); the coefficients
-// are stored as duplicated pairs so that each packed FMA reads one 64-bit constant.
-#if !DEGPU_PARITY && DEGPU_N >= 2 && DEGPU_ALG == 0
-#define DEGPU_PACKED 1
+// packed (fast mode) Tsit5 tables: the coefficients as duplicated pairs, and the dense-output
+// polynomial coefficients of stage pairs
+#if DEGPU_PACKED && DEGPU_ALG == 0
 #define DEGPU_X_F2(v) {(float)(v), (float)(v)},
 __constant__ float2 c_tsit5_2[TS_COUNT] = {DEGPU_TSIT5_VALUES(DEGPU_X_F2)};
 // dense-output coefficients of the stage pairs (2,3), (4,5), (6,7): {(r_j2, r_j+1,2), (.3), (.4)}
@@ -190,8 +197,6 @@ constexpr float kTs[TS_COUNT] = {DEGPU_TSIT5_VALUES(DEGPU_X_F)};
 #define DEGPU_RP(a, b) {{kTs[TS_r##a##2], kTs[TS_r##b##2]}, {kTs[TS_r##a##3], kTs[TS_r##b##3]}, {kTs[TS_r##a##4], kTs[TS_r##b##4]}}
 __constant__ float2 c_tsit5_rp[3][3] = {DEGPU_RP(2, 3), DEGPU_RP(4, 5), DEGPU_RP(6, 7)};
 #undef DEGPU_RP
-#else
-#define DEGPU_PACKED 0
 #endif
 #define TS(n) c_tsit5[TS_##n]
 #define V7(n) c_vern7[VERN7_##n]
@@ -218,6 +223,50 @@ DEGPU_DEV float ctrl_pow(float x, float y) {
 
 
 DEGPU_DEV void rhs(float* du, const float* u, const float* p, float t) { degpu_f<float>(du, u, p, t); }
+
+#if DEGPU_PACKED
+// A stage sum sum_j c_j k_j over the state components, two components per packed
+// instruction (the last component of an odd N takes the scalar FMA), accumulated left to
+// right: psum_first then psum_add per term; each term passes its coefficient as the
+// duplicated pair and the scalar.
+constexpr int NP2 = N / 2 > 0 ? N / 2 : 1;
+struct PSum {
+  float2 s2[NP2];
+  float s1;
+};
+DEGPU_DEV void psum_first(PSum& a, float2 c2, float c, const float* kv) {
+#pragma unroll
+  for (int i = 0; i + 1 < N; i += 2) a.s2[i / 2] = __fmul2_rn(c2, make_float2(kv[i], kv[i + 1]));
+  if (N & 1) a.s1 = c * kv[N - 1];
+}
+DEGPU_DEV void psum_add(PSum& a, float2 c2, float c, const float* kv) {
+#pragma unroll
+  for (int i = 0; i + 1 < N; i += 2) a.s2[i / 2] = __ffma2_rn(c2, make_float2(kv[i], kv[i + 1]), a.s2[i / 2]);
+  if (N & 1) a.s1 = fmaf(c, kv[N - 1], a.s1);
+}
+// out = up + dt * sum
+DEGPU_DEV void psum_stage(float* out, const float* up, float dt, const PSum& a) {
+  const float2 dt2 = make_float2(dt, dt);
+#pragma unroll
+  for (int i = 0; i + 1 < N; i += 2) {
+    const float2 r = __ffma2_rn(dt2, a.s2[i / 2], make_float2(up[i], up[i + 1]));
+    out[i] = r.x;
+    out[i + 1] = r.y;
+  }
+  if (N & 1) out[N - 1] = fmaf(dt, a.s1, up[N - 1]);
+}
+// out = dt * sum
+DEGPU_DEV void psum_scaled(float* out, float dt, const PSum& a) {
+  const float2 dt2 = make_float2(dt, dt);
+#pragma unroll
+  for (int i = 0; i + 1 < N; i += 2) {
+    const float2 r = __fmul2_rn(dt2, a.s2[i / 2]);
+    out[i] = r.x;
+    out[i + 1] = r.y;
+  }
+  if (N & 1) out[N - 1] = dt * a.s1;
+}
+#endif
 
 // DiffEqBase.ODE_DEFAULT_NORM on a static vector: sqrt(sum(abs2, x) / length(x))
 DEGPU_DEV float scaled_norm(const float* e, const float* up, const float* u, float abstol, float reltol) {
@@ -642,11 +691,72 @@ DEGPU_DEV void begin_step(Lane& L, bool) {
   // not FSAL: k1 = f(uprev, p, t) every step (:30, :117; one evaluation per step suffices)
   rhs(L.k[0], L.uprev, L.p, TP::f32(L.t));
 }
+#if DEGPU_PACKED
+// one Vern7 coefficient as a packed-sum term: (duplicated pair, scalar)
+#define V7P(n) c_vern7_2[VERN7_##n], c_vern7[VERN7_##n]
+#endif
 template <bool ADAPTIVE>
 DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
   float tmp[N];
   const float* up = L.uprev;
   float(*k)[N] = L.k;
+#if DEGPU_PACKED
+  {  // gpu_vern7_perform_step.jl:118-151 (:31-56 fixed step), two components per instruction
+    PSum s;
+    const float a = dt * V7(a021);
+    const float2 a2 = make_float2(a, a);
+#pragma unroll
+    for (int i = 0; i + 1 < N; i += 2) {  // tmp = uprev + (dt a21) k1
+      const float2 r = __ffma2_rn(a2, make_float2(k[0][i], k[0][i + 1]), make_float2(up[i], up[i + 1]));
+      tmp[i] = r.x;
+      tmp[i + 1] = r.y;
+    }
+    if (N & 1) tmp[N - 1] = fmaf(a, k[0][N - 1], up[N - 1]);
+    rhs(k[1], tmp, L.p, tstage(t, V7(c2), dt));
+    psum_first(s, V7P(a031), k[0]); psum_add(s, V7P(a032), k[1]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[2], tmp, L.p, tstage(t, V7(c3), dt));
+    psum_first(s, V7P(a041), k[0]); psum_add(s, V7P(a043), k[2]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[3], tmp, L.p, tstage(t, V7(c4), dt));
+    psum_first(s, V7P(a051), k[0]); psum_add(s, V7P(a053), k[2]); psum_add(s, V7P(a054), k[3]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[4], tmp, L.p, tstage(t, V7(c5), dt));
+    psum_first(s, V7P(a061), k[0]); psum_add(s, V7P(a063), k[2]); psum_add(s, V7P(a064), k[3]);
+    psum_add(s, V7P(a065), k[4]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[5], tmp, L.p, tstage(t, V7(c6), dt));
+    psum_first(s, V7P(a071), k[0]); psum_add(s, V7P(a073), k[2]); psum_add(s, V7P(a074), k[3]);
+    psum_add(s, V7P(a075), k[4]); psum_add(s, V7P(a076), k[5]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[6], tmp, L.p, tstage(t, V7(c7), dt));
+    psum_first(s, V7P(a081), k[0]); psum_add(s, V7P(a083), k[2]); psum_add(s, V7P(a084), k[3]);
+    psum_add(s, V7P(a085), k[4]); psum_add(s, V7P(a086), k[5]); psum_add(s, V7P(a087), k[6]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[7], tmp, L.p, tstage(t, V7(c8), dt));
+    float g10[N];
+    psum_first(s, V7P(a091), k[0]); psum_add(s, V7P(a093), k[2]); psum_add(s, V7P(a094), k[3]);
+    psum_add(s, V7P(a095), k[4]); psum_add(s, V7P(a096), k[5]); psum_add(s, V7P(a097), k[6]);
+    psum_add(s, V7P(a098), k[7]);
+    psum_stage(tmp, up, dt, s);
+    psum_first(s, V7P(a101), k[0]); psum_add(s, V7P(a103), k[2]); psum_add(s, V7P(a104), k[3]);
+    psum_add(s, V7P(a105), k[4]); psum_add(s, V7P(a106), k[5]); psum_add(s, V7P(a107), k[6]);
+    psum_stage(g10, up, dt, s);
+    rhs(k[8], tmp, L.p, tstage(t, 1.0f, dt));
+    rhs(k[9], g10, L.p, tstage(t, 1.0f, dt));
+    psum_first(s, V7P(b1), k[0]); psum_add(s, V7P(b4), k[3]); psum_add(s, V7P(b5), k[4]);
+    psum_add(s, V7P(b6), k[5]); psum_add(s, V7P(b7), k[6]); psum_add(s, V7P(b8), k[7]);
+    psum_add(s, V7P(b9), k[8]);
+    psum_stage(u, up, dt, s);
+    if (ADAPTIVE) {
+      psum_first(s, V7P(btilde1), k[0]); psum_add(s, V7P(btilde4), k[3]); psum_add(s, V7P(btilde5), k[4]);
+      psum_add(s, V7P(btilde6), k[5]); psum_add(s, V7P(btilde7), k[6]); psum_add(s, V7P(btilde8), k[7]);
+      psum_add(s, V7P(btilde9), k[8]); psum_add(s, V7P(btilde10), k[9]);
+      psum_scaled(err, dt, s);
+    }
+    return;
+  }
+#endif
   float a = dt * V7(a021);
 #pragma unroll
   for (int i = 0; i < N; i++) tmp[i] = up[i] + a * k[0][i];
@@ -995,11 +1105,100 @@ DEGPU_DEV void begin_step(Lane& L, bool) {
   // not FSAL: k1 = f(uprev, p, t) every step (:33, :170; one evaluation per step suffices)
   rhs(L.k[0], L.uprev, L.p, TP::f32(L.t));
 }
+#if DEGPU_PACKED
+// one Vern9 coefficient as a packed-sum term: (duplicated pair, scalar)
+#define V9P(n) c_vern9_2[VERN9_##n], c_vern9[VERN9_##n]
+#endif
 template <bool ADAPTIVE>
 DEGPU_DEV void attempt(Lane& L, Time t, float dt, float* u, float* err) {
   float tmp[N], k2[N], k3[N], k4[N], k5[N], k6[N], k7[N];
   const float* up = L.uprev;
   float(*k)[N] = L.k;
+#if DEGPU_PACKED
+  {  // gpu_vern9_perform_step.jl, two components per instruction (terms left to right as above)
+    PSum s;
+    float g16[N];
+    const float a = dt * V9(a0201);
+    const float2 a2 = make_float2(a, a);
+#pragma unroll
+    for (int i = 0; i + 1 < N; i += 2) {  // tmp = uprev + (dt a0201) k1
+      const float2 r = __ffma2_rn(a2, make_float2(k[0][i], k[0][i + 1]), make_float2(up[i], up[i + 1]));
+      tmp[i] = r.x;
+      tmp[i + 1] = r.y;
+    }
+    if (N & 1) tmp[N - 1] = fmaf(a, k[0][N - 1], up[N - 1]);
+    rhs(k2, tmp, L.p, tstage(t, V9(c1), dt));
+    psum_first(s, V9P(a0301), k[0]); psum_add(s, V9P(a0302), k2);
+    psum_stage(tmp, up, dt, s);
+    rhs(k3, tmp, L.p, tstage(t, V9(c2), dt));
+    psum_first(s, V9P(a0401), k[0]); psum_add(s, V9P(a0403), k3);
+    psum_stage(tmp, up, dt, s);
+    rhs(k4, tmp, L.p, tstage(t, V9(c3), dt));
+    psum_first(s, V9P(a0501), k[0]); psum_add(s, V9P(a0503), k3); psum_add(s, V9P(a0504), k4);
+    psum_stage(tmp, up, dt, s);
+    rhs(k5, tmp, L.p, tstage(t, V9(c4), dt));
+    psum_first(s, V9P(a0601), k[0]); psum_add(s, V9P(a0604), k4); psum_add(s, V9P(a0605), k5);
+    psum_stage(tmp, up, dt, s);
+    rhs(k6, tmp, L.p, tstage(t, V9(c5), dt));
+    psum_first(s, V9P(a0701), k[0]); psum_add(s, V9P(a0704), k4); psum_add(s, V9P(a0705), k5);
+    psum_add(s, V9P(a0706), k6);
+    psum_stage(tmp, up, dt, s);
+    rhs(k7, tmp, L.p, tstage(t, V9(c6), dt));
+    psum_first(s, V9P(a0801), k[0]); psum_add(s, V9P(a0806), k6); psum_add(s, V9P(a0807), k7);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[1], tmp, L.p, tstage(t, V9(c7), dt));
+    psum_first(s, V9P(a0901), k[0]); psum_add(s, V9P(a0906), k6); psum_add(s, V9P(a0907), k7);
+    psum_add(s, V9P(a0908), k[1]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[2], tmp, L.p, tstage(t, V9(c8), dt));
+    psum_first(s, V9P(a1001), k[0]); psum_add(s, V9P(a1006), k6); psum_add(s, V9P(a1007), k7);
+    psum_add(s, V9P(a1008), k[1]); psum_add(s, V9P(a1009), k[2]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[3], tmp, L.p, tstage(t, V9(c9), dt));
+    psum_first(s, V9P(a1101), k[0]); psum_add(s, V9P(a1106), k6); psum_add(s, V9P(a1107), k7);
+    psum_add(s, V9P(a1108), k[1]); psum_add(s, V9P(a1109), k[2]); psum_add(s, V9P(a1110), k[3]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[4], tmp, L.p, tstage(t, V9(c10), dt));
+    psum_first(s, V9P(a1201), k[0]); psum_add(s, V9P(a1206), k6); psum_add(s, V9P(a1207), k7);
+    psum_add(s, V9P(a1208), k[1]); psum_add(s, V9P(a1209), k[2]); psum_add(s, V9P(a1210), k[3]);
+    psum_add(s, V9P(a1211), k[4]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[5], tmp, L.p, tstage(t, V9(c11), dt));
+    psum_first(s, V9P(a1301), k[0]); psum_add(s, V9P(a1306), k6); psum_add(s, V9P(a1307), k7);
+    psum_add(s, V9P(a1308), k[1]); psum_add(s, V9P(a1309), k[2]); psum_add(s, V9P(a1310), k[3]);
+    psum_add(s, V9P(a1311), k[4]); psum_add(s, V9P(a1312), k[5]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[6], tmp, L.p, tstage(t, V9(c12), dt));
+    psum_first(s, V9P(a1401), k[0]); psum_add(s, V9P(a1406), k6); psum_add(s, V9P(a1407), k7);
+    psum_add(s, V9P(a1408), k[1]); psum_add(s, V9P(a1409), k[2]); psum_add(s, V9P(a1410), k[3]);
+    psum_add(s, V9P(a1411), k[4]); psum_add(s, V9P(a1412), k[5]); psum_add(s, V9P(a1413), k[6]);
+    psum_stage(tmp, up, dt, s);
+    rhs(k[7], tmp, L.p, tstage(t, V9(c13), dt));
+    psum_first(s, V9P(a1501), k[0]); psum_add(s, V9P(a1506), k6); psum_add(s, V9P(a1507), k7);
+    psum_add(s, V9P(a1508), k[1]); psum_add(s, V9P(a1509), k[2]); psum_add(s, V9P(a1510), k[3]);
+    psum_add(s, V9P(a1511), k[4]); psum_add(s, V9P(a1512), k[5]); psum_add(s, V9P(a1513), k[6]);
+    psum_add(s, V9P(a1514), k[7]);
+    psum_stage(tmp, up, dt, s);
+    psum_first(s, V9P(a1601), k[0]); psum_add(s, V9P(a1606), k6); psum_add(s, V9P(a1607), k7);
+    psum_add(s, V9P(a1608), k[1]); psum_add(s, V9P(a1609), k[2]); psum_add(s, V9P(a1610), k[3]);
+    psum_add(s, V9P(a1611), k[4]); psum_add(s, V9P(a1612), k[5]); psum_add(s, V9P(a1613), k[6]);
+    psum_stage(g16, up, dt, s);
+    rhs(k[8], tmp, L.p, tstage(t, 1.0f, dt));
+    rhs(k[9], g16, L.p, tstage(t, 1.0f, dt));
+    psum_first(s, V9P(b1), k[0]); psum_add(s, V9P(b8), k[1]); psum_add(s, V9P(b9), k[2]);
+    psum_add(s, V9P(b10), k[3]); psum_add(s, V9P(b11), k[4]); psum_add(s, V9P(b12), k[5]);
+    psum_add(s, V9P(b13), k[6]); psum_add(s, V9P(b14), k[7]); psum_add(s, V9P(b15), k[8]);
+    psum_stage(u, up, dt, s);
+    if (ADAPTIVE) {
+      psum_first(s, V9P(btilde1), k[0]); psum_add(s, V9P(btilde8), k[1]); psum_add(s, V9P(btilde9), k[2]);
+      psum_add(s, V9P(btilde10), k[3]); psum_add(s, V9P(btilde11), k[4]); psum_add(s, V9P(btilde12), k[5]);
+      psum_add(s, V9P(btilde13), k[6]); psum_add(s, V9P(btilde14), k[7]); psum_add(s, V9P(btilde15), k[8]);
+      psum_add(s, V9P(btilde16), k[9]);
+      psum_scaled(err, dt, s);
+    }
+    return;
+  }
+#endif
   float a = dt * V9(a0201);
 #pragma unroll
   for (int i = 0; i < N; i++) tmp[i] = up[i] + a * k[0][i];

@@ -97,6 +97,10 @@ def f32_literal(x: float) -> str:
     return s + "f"
 
 
+# tables whose stage sums the fast-mode kernels evaluate two state components at a time
+PACKED = ("vern7", "vern9")
+
+
 def main():
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     oracle_lines = [
@@ -141,6 +145,14 @@ def main():
         for n, v in entries:
             dev_lines.append(f"  {f32_literal(v)}, // {n}")
         dev_lines.append("};")
+        if tab in PACKED:
+            # the same values as duplicated pairs, for the packed FP32 stage sums of fast mode
+            dev_lines.append("#if DEGPU_PACKED_TABLES")
+            dev_lines.append(f"__constant__ float2 c_{tab}_2[{tab.upper()}_COUNT] = {{")
+            for n, v in entries:
+                dev_lines.append(f"  {{{f32_literal(v)}, {f32_literal(v)}}}, // {n}")
+            dev_lines.append("};")
+            dev_lines.append("#endif")
         dev_lines.append("")
     (REPO / "oracle" / "tableaus_gen.h").write_text("\n".join(oracle_lines) + "\n")
     (REPO / "diffeqgpu.jl_gb300" / "csrc" / "device" / "tableaus_gen.cuh").write_text("\n".join(dev_lines) + "\n")
