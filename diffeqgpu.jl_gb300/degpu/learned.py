@@ -350,12 +350,18 @@ def work_order(work, stream=None):
     return order
 
 
-def predicted_work(model, u0_dev, p_dev, reltol):
-    """Predicted step attempts (device float32 [B]) of a work model on device (u0, p)."""
+def predicted_work(model, u0_dev, p_dev, reltol, span_dev=None):
+    """Predicted step attempts (device float32 [B]) of a work model on device (u0, p) and,
+    for a model trained with per-trajectory tspans, the spans tf - t0 (device [B])."""
     import torch
     B = u0_dev.shape[0]
-    x = torch.cat([u0_dev.float(), p_dev.float().reshape(B, -1),
-                   torch.full((B, 1), float(np.log10(reltol)), dtype=torch.float32, device=u0_dev.device)], 1)
+    cols = [u0_dev.float(), p_dev.float().reshape(B, -1),
+            torch.full((B, 1), float(np.log10(reltol)), dtype=torch.float32, device=u0_dev.device)]
+    if span_dev is not None:
+        cols.append(span_dev.float().reshape(B, 1))
+    x = torch.cat(cols, 1)
+    if x.shape[1] != model.n_in:
+        raise ValueError(f"the work model takes {model.n_in} inputs, got {x.shape[1]} (span_dev for spans?)")
     y = model.infer(x.contiguous(), raw=True)
     return torch.exp(y[:, 0]).clamp(1.0, 2.0 ** 31)
 
