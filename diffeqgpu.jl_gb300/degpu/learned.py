@@ -8,13 +8,14 @@ predictions into a longest-first visiting order for the persistent driver, which
 the drain at the end of an ensemble with uneven step counts.  Results do not depend on the
 order; only the schedule does.
 
-Targets, from two plain solves of the training ensemble (both on the GPU):
+Step-model targets, from plain solves of the training ensemble (all on the GPU):
   * log dt0    -- the first step the plain controller accepted (accepted-step trace);
   * log scale  -- how far the trajectory's tolerances can be relaxed before its final-state
-    error reaches a common target: err_i is the plain solution's distance to a 32x
-    tighter plain solve, scale_i = clip((target / err_i)^(1/alpha), 1, s_max).  Scales
-    are >= 1: the learned run is never asked for tighter tolerances than the plain run,
-    and members whose error already exceeds the target (chaotic ones) keep the plain
+    error reaches a common target: err_i(s) is the distance of the plain solution at
+    tolerance scale s (1, 2, 4, ..., 64) to a 64x tighter plain solve, and the target scale
+    is the largest s whose error, and that of every smaller s, stays at or below the target.
+    Scales are >= 1: the learned run is never asked for tighter tolerances than the plain
+    run, and members the plain run does not resolve (chaotic ones) keep the plain
     tolerances.  The embedded error estimate still accepts or rejects every step.
 """
 from __future__ import annotations
@@ -190,17 +191,6 @@ class StepSizeModel:
             p[o_b3:] = (b3 * t_sd + t_mu).astype(np.float32)
             self.set(p, mu, sd)
         return hist
-
-
-def training_targets(first_dt, err, target_err, *, alpha=1.0, s_max=1e3, err_floor=1e-9):
-    """(log dt0, log scale) targets and weights from the plain solver's traces."""
-    first_dt = np.asarray(first_dt, np.float64)
-    err = np.maximum(np.asarray(err, np.float64), err_floor)
-    ok = np.isfinite(first_dt) & (first_dt > 0) & np.isfinite(err)
-    scale = np.clip((target_err / err) ** (1.0 / alpha), 1.0, s_max)
-    y = np.stack([np.log(np.where(ok, first_dt, 1.0)), np.log(scale)], 1).astype(np.float32)
-    w = np.stack([ok, ok], 1).astype(np.float32)
-    return y, w
 
 
 def solver_traces(f, u0, p, tspan, time_type, alg, *, reltol, abstol, dt=0.1, scales=(1, 2, 4, 8, 16, 32, 64),
