@@ -744,7 +744,8 @@ def gpu_arm(args):
                      "peak_source": "measured live: FP32 FMA probe (degpu_fp32_peak)",
                      "flops_per_launch": best_rec["flops_per_launch"],
                      "attempts_per_traj": best_rec["attempts_per_traj"],
-                     "plain_index_order_frac": fl / (ms_plain / args.steps * 1e-3) / 1e12 / peak.value},
+                     "plain_index_order_frac": fl / (ms_plain / args.steps * 1e-3) / 1e12 / peak.value,
+                     "hbm_view": hbm_view(traffic, best_rec["ms_per_step"] * 1e-3)},
         "e2e": e2e,
         "e2e_plain": e2e_plain,
         "cpu_baseline": cpu,
@@ -789,6 +790,19 @@ def profile_case(args):
     same = bool(torch.equal(r.us, r2.us))
     print(json.dumps({"profile_case": args.profile_case, "trajectories": B, "ms": e0.elapsed_time(e1),
                       "attempts_per_traj": float((r.naccept + r.nreject).float().mean()), "same_as_index_order": same}))
+
+
+def hbm_view(traffic_bytes, seconds):
+    """The dominant kernel's DRAM traffic rate against the measured copy bandwidth of
+    MEASURED_PEAKS.json (when present): the evidence that the FP32-issue-bound kernel is
+    not bandwidth-bound."""
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        peak = float(peaks["hbm_gbs"])
+    except Exception:
+        return None
+    gbs = traffic_bytes / seconds / 1e9
+    return {"achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}
 
 
 # see the traffic note in gpu_arm
